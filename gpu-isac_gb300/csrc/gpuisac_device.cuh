@@ -1,0 +1,205 @@
+// gpuisac_device.cuh -- device building blocks shared by the alignment kernels:
+// complex helpers, the 16-point DFT, the 256-point FFT split over 16 threads,
+// and the texture-unit-faithful bilinear sampler of the stacked image arrays.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpuisac {
+
+constexpr int kRingLen = 256;        // polar samples per ring (angles)
+constexpr int kSlots = kRingLen / 2; // spectrum slots per ring: k = 1..127, slot 0 = (F[0], F[128])
+constexpr int kFftGroup = 16;        // threads per 256-point FFT
+constexpr int kPairStride = 272;     // float2 per FFT workspace (16 x 17, padded transpose)
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// multiply by +i (SIGN>0) or -i (SIGN<0)
+template <int SIGN>
+__device__ __forceinline__ float2 cmul_i(float2 a)
+{
+    return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// 4-point DFT in place, X[k] = sum_n x[n] w4^(SIGN n k), w4 = e^(2 pi i / 4)
+template <int SIGN>
+__device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3)
+{
+    float2 a = cadd(x0, x2), b = csub(x0, x2);
+    float2 c = cadd(x1, x3), d = cmul_i<SIGN>(csub(x1, x3));
+    x0 = cadd(a, c);
+    x2 = csub(a, c);
+    x1 = cadd(b, d);
+    x3 = csub(b, d);
+}
+
+// e^(SIGN 2 pi i m / 16) for m = 0..9 (cos/sin of multiples of 22.5 degrees)
+template <int SIGN>
+__device__ __forceinline__ float2 w16(int m)
+{
+    const float c1 = 0.923879532511286756f, s1 = 0.382683432365089772f, c2 = 0.707106781186547524f;
+    float2 r;
+    switch (m) {
+    case 0: r = make_float2(1.f, 0.f); break;
+    case 1: r = make_float2(c1, s1); break;
+    case 2: r = make_float2(c2, c2); break;
+    case 3: r = make_float2(s1, c1); break;
+    case 4: r = make_float2(0.f, 1.f); break;
+    case 6: r = make_float2(-c2, c2); break;
+    case 9: r = make_float2(-c1, -s1); break;
+    default: r = make_float2(1.f, 0.f); break;
+    }
+    r.y *= (float)SIGN;
+    return r;
+}
+
+// 16-point DFT in registers, natural order in and out:
+// X[k] = sum_n x[n] e^(SIGN 2 pi i n k / 16); 16 = 4 x 4 with twiddles w16^(n1 k1)
+template <int SIGN>
+__device__ __forceinline__ void dft16(float2 (&x)[16])
+{
+    // stage 1: for each n1, 4-point DFT over n2 of x[n1 + 4 n2] -> T[n1][k1]
+#pragma unroll
+    for (int n1 = 0; n1 < 4; n1++)
+        dft4<SIGN>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
+    // x[n1 + 4 k1] now holds T[n1][k1]; twiddle by w16^(n1 k1)
+#pragma unroll
+    for (int n1 = 1; n1 < 4; n1++)
+#pragma unroll
+        for (int k1 = 1; k1 < 4; k1++)
+            x[n1 + 4 * k1] = cmul(x[n1 + 4 * k1], w16<SIGN>(n1 * k1));
+    // stage 2: for each k1, 4-point DFT over n1 -> X[k1 + 4 k2]
+    float2 y[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+        float2 a0 = x[0 + 4 * k1], a1 = x[1 + 4 * k1], a2 = x[2 + 4 * k1], a3 = x[3 + 4 * k1];
+        dft4<SIGN>(a0, a1, a2, a3);
+        y[k1 + 0] = a0;
+        y[k1 + 4] = a1;
+        y[k1 + 8] = a2;
+        y[k1 + 12] = a3;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        x[i] = y[i];
+}
+
+// 256-point complex FFT over a group of 16 threads (thread l = 0..15).
+// In:  x[m] = z[l + 16 m].
+// Out: x[k2] = Z[l + 16 k2],  Z[k] = sum_n z[n] e^(SIGN 2 pi i n k / 256).
+// ws: this group's workspace of kPairStride float2; tw: e^(-2 pi i e / 256),
+// e = 0..255 (forward twiddles; the inverse conjugates them).
+// Every thread of the group must call; mask = the group's lanes.
+template <int SIGN>
+__device__ __forceinline__ void fft256_group(float2 (&x)[16], float2* ws, const float2* tw, int l,
+                                             unsigned mask)
+{
+    dft16<SIGN>(x);
+    // twiddle w256^(SIGN l j)
+#pragma unroll
+    for (int j = 1; j < 16; j++) {
+        float2 w = tw[(l * j) & 255];
+        w.y *= (float)(-SIGN); // table holds e^(-...), flip for SIGN=+1
+        x[j] = cmul(x[j], w);
+    }
+    // transpose through shared memory (row stride 17 avoids bank conflicts)
+    __syncwarp(mask);
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+        ws[l * 17 + j] = x[j];
+    __syncwarp(mask);
+#pragma unroll
+    for (int n = 0; n < 16; n++)
+        x[n] = ws[n * 17 + l];
+    __syncwarp(mask);
+    dft16<SIGN>(x);
+}
+
+// ---------------------------------------------------------------------------
+// Stacked image arrays read the way the reference's 2D textures are read
+// (bilinear, clamp, unnormalised coordinates; cuda/gpu_aln_noref.cu:1258-1286,
+// 2314-2339): images are grouped in batches of `batch`, each batch in textures
+// of `tex` images; a bilinear tap below/above an image reads the neighbouring
+// image of the same texture, the ends of a texture clamp, and texture slots a
+// short final batch leaves untouched still hold the previous batch's images.
+struct StackDesc {
+    const float* img; // [n][dim][dim]
+    unsigned n, dim, batch, tex;
+};
+
+struct TexPlacement {
+    unsigned local;      // image index inside its texture (the reference's block index)
+    unsigned tex_first;  // global index of the texture's slot 0
+    unsigned batch_end;  // one past the last image of the current batch
+    long rows;           // texture height in rows
+};
+
+__device__ __forceinline__ TexPlacement tex_place(const StackDesc& s, unsigned img)
+{
+    TexPlacement t;
+    unsigned bstart = (img / s.batch) * s.batch;
+    unsigned blen = min(s.batch, s.n - bstart);
+    unsigned loc = img - bstart;
+    unsigned tex_idx = loc / s.tex;
+    unsigned n_tex_alloc = (s.batch + s.tex - 1) / s.tex;
+    unsigned alloc = (tex_idx != n_tex_alloc - 1) ? s.tex : s.batch - tex_idx * s.tex;
+    t.local = loc - tex_idx * s.tex;
+    t.tex_first = bstart + tex_idx * s.tex;
+    t.batch_end = bstart + blen;
+    t.rows = (long)alloc * s.dim;
+    return t;
+}
+
+__device__ __forceinline__ const float* tex_row(const StackDesc& s, const TexPlacement& t, long row)
+{
+    row = row < 0 ? 0 : (row > t.rows - 1 ? t.rows - 1 : row);
+    unsigned slot = (unsigned)(row / s.dim);
+    unsigned yy = (unsigned)(row - (long)slot * s.dim);
+    unsigned g = t.tex_first + slot;
+    if (g >= t.batch_end)
+        g -= s.batch; // slot not refilled by a short final batch
+    return s.img + ((size_t)g * s.dim + yy) * s.dim;
+}
+
+// fixed-point split of a texel-space coordinate: 8 fractional bits, round to
+// nearest even (same rule as the oracle's orc_tex_split)
+__device__ __forceinline__ void tex_split(float t, int& i, float& a)
+{
+    int q = __float2int_rn((t - 0.5f) * 256.0f);
+    i = q >> 8;
+    a = (float)(q & 255) * (1.0f / 256.0f);
+}
+
+__device__ __forceinline__ float tex_sample(const StackDesc& s, const TexPlacement& t, float x, float y)
+{
+    int ix, iy;
+    float ax, ay;
+    tex_split(x, ix, ax);
+    tex_split(y, iy, ay);
+    int dm1 = (int)s.dim - 1;
+    int x0 = min(max(ix, 0), dm1), x1 = min(max(ix + 1, 0), dm1);
+    const float* r0 = tex_row(s, t, iy);
+    const float* r1 = tex_row(s, t, (long)iy + 1);
+    float t00 = __ldg(r0 + x0), t10 = __ldg(r0 + x1);
+    float t01 = __ldg(r1 + x0), t11 = __ldg(r1 + x1);
+    return (1.f - ax) * (1.f - ay) * t00 + ax * (1.f - ay) * t10 + (1.f - ax) * ay * t01 + ax * ay * t11;
+}
+
+// Reference: polar grid centre, cuda/gpu_aln_noref.cu:1262-1269 (D/2 + shift in
+// unsigned arithmetic, base shift added in float, +0.5 in double, stored float)
+__device__ __forceinline__ float centre_coord(unsigned dim, int shift, const float* base)
+{
+    unsigned u = dim / 2u + (unsigned)shift;
+    if (base) {
+        float f = (float)u + *base;
+        return (float)((double)f + 0.5);
+    }
+    return (float)((double)u + 0.5);
+}
+
+} // namespace gpuisac

@@ -1,0 +1,50 @@
+// gpuisac_kernels.h -- host-side launchers of the alignment kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include <atomic>
+
+#include "gpuisac_device.cuh"
+
+namespace gpuisac {
+
+constexpr unsigned kMaxRingNum = 88;    // rings supported by the kernels (reference tile fits shared memory)
+constexpr unsigned kMaxShifts = 4096;   // shift grid entries supported
+
+inline size_t polar_spectra_smem_bytes(unsigned ring_num)
+{
+    return (size_t)ring_num * kRingLen * sizeof(float) + 16 * kPairStride * sizeof(float2) +
+           kRingLen * sizeof(float2) + 24 * sizeof(double);
+}
+
+// rings are padded to a multiple of this in the reference tile in shared memory
+constexpr unsigned kRingPad = 8;
+__host__ __device__ inline unsigned ring_pad(unsigned ring_num) { return (ring_num + kRingPad - 1) / kRingPad * kRingPad; }
+
+// references per CTA of the CCF/peak kernel for a ring count
+inline unsigned ccf_refs_per_cta(unsigned ring_num) { return ring_pad(ring_num) <= 40 ? 4u : 2u; }
+
+size_t ccf_peak_smem_bytes(unsigned ring_num);
+
+// kernels launched by this library since load (all launchers count here)
+extern std::atomic<unsigned long long> g_kernel_launches;
+
+// Resample + normalise + ring FFT of n_img images x n_shift shifts.
+// out: [n_img][n_shift][ring_num][kSlots] float2 (see polar_spectra.cu).
+cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
+                                 unsigned ring_num, const int2* shift_int, unsigned n_shift,
+                                 const float2* base, unsigned img0, unsigned n_img, int is_ref,
+                                 float2* out, cudaStream_t stream);
+
+// CCF against every reference + inverse FFT + peak search for n_part particles
+// whose spectra are in sbj_sp ([n_part][n_shift][ring_num][kSlots]); results
+// for particle i go to column p_global0 + i of d_out [n_ref][p_total] and
+// peak_out [n_ref][p_total] (angle, shift_x, shift_y, mirror).
+cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle,
+                            unsigned ring_num, unsigned n_shift, unsigned n_ref, unsigned n_part,
+                            unsigned p_global0, unsigned p_total, const float2* shifts_f,
+                            const float2* base, float* d_out, float4* peak_out, cudaStream_t stream);
+
+} // namespace gpuisac

@@ -1,0 +1,166 @@
+// polar_spectra.cu -- polar resampling, per-image normalisation and per-ring
+// real FFT of images (one CTA per image x shift), written straight in the
+// basis the CCF contraction consumes.
+//
+// Reference semantics: cu_resample_to_polar (cuda/gpu_aln_noref.cu:1221-1354)
+// followed by the in-place R2C cuFFT of every ring (:2121-2125).
+//
+// Output, per (image, shift) row, [ring][slot] float2:
+//   slot k = 1..127 holds F[k]; slot 0 holds (F[0], F[128]) (both real);
+//   subjects store (Re+Im, Re-Im)            of that pair of numbers,
+//   references store (r+1) * (Re+Im, Re-Im)  (the ring weight folded in).
+// With refs (u, v) and subjects (a, b) the four sums sum_r u a, u b, v b, v a
+// are exactly Re/Im of Z[k] = O[k] + i M[k] and of Z[256-k], the spectrum
+// whose inverse FFT gives the normal (real part) and mirrored (imaginary
+// part) correlation at once.
+#include "gpuisac_device.cuh"
+#include "gpuisac_kernels.h"
+
+namespace gpuisac {
+
+std::atomic<unsigned long long> g_kernel_launches{0};
+
+__global__ void __launch_bounds__(256)
+polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
+                     unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
+                     const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
+                     float2* __restrict__ out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* polar = reinterpret_cast<float*>(smem_raw);                        // [ring_num][256]
+    float2* ws = reinterpret_cast<float2*>(polar + ring_num * kRingLen);      // 16 x kPairStride
+    float2* tw = ws + 16 * kPairStride;                                       // 256
+    double* red = reinterpret_cast<double*>(tw + kRingLen);                   // 2 x 8 warps + 2
+
+    const unsigned row = blockIdx.x;
+    const unsigned img_local = row / n_shift;
+    const unsigned s = row - img_local * n_shift;
+    if (img_local >= n_img)
+        return;
+    const unsigned img = img0 + img_local;
+    const int tid = threadIdx.x;
+
+    tw[tid] = twiddle[tid];
+
+    // ---- sampling positions exactly as the reference computes them ----
+    const int2 sh = shift_int[s];
+    const float* bx = base ? &base[img].x : nullptr;
+    const float* by = base ? &base[img].y : nullptr;
+    const float cnt_x = centre_coord(st.dim, sh.x, bx);
+    const float cnt_y = centre_coord(st.dim, sh.y, by);
+    const TexPlacement place = tex_place(st, img);
+    const float yoff = (float)(place.local * st.dim);
+
+    // thread tid samples angle tid of every ring; FP32 ring-weighted partial
+    // sums feed the FP64 image mean / deviation
+    float s1 = 0.f, s2 = 0.f;
+    for (unsigned r = 0; r < ring_num; r++) {
+        float2 o = __ldg(&tmpl[r * kRingLen + tid]);
+        float x = cnt_x + o.x;
+        float y = (yoff + cnt_y) + o.y;
+        float v = tex_sample(st, place, x, y);
+        polar[r * kRingLen + tid] = v;
+        float w = (float)(r + 1);
+        s1 += w * v;
+        s2 += w * v * v;
+    }
+    double d1 = s1, d2 = s2;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        d1 += __shfl_xor_sync(0xffffffffu, d1, off);
+        d2 += __shfl_xor_sync(0xffffffffu, d2, off);
+    }
+    const int warp = tid >> 5, lane = tid & 31;
+    if (lane == 0) {
+        red[warp] = d1;
+        red[8 + warp] = d2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0.0, q = 0.0;
+        for (int w = 0; w < 8; w++) {
+            a += red[w];
+            q += red[8 + w];
+        }
+        // avg = sum (r+1) A_r / (L sum (r+1)); same for the squares (noref.cu:1314-1337)
+        double nn = 0.5 * (double)ring_num * (double)(ring_num + 1) * (double)kRingLen;
+        double avg = a / nn, msq = q / nn;
+        double sd = sqrt(fabs(msq - avg * avg));
+        red[16] = avg;
+        red[17] = 1.0 / (sd + 0.0000001);
+    }
+    __syncthreads();
+    const float avg_f = (float)red[16], inv_f = (float)red[17];
+
+    // ---- per-ring FFT, two rings per complex 256-point FFT ----
+    const int g = tid >> 4;          // FFT group 0..15
+    const int l = tid & 15;
+    const unsigned gmask = 0xffffu << (tid & 16);
+    float2* gws = ws + g * kPairStride;
+    const unsigned n_pairs = (ring_num + 1) / 2;
+    float2* out_row = out + (size_t)row * ring_num * kSlots;
+    for (unsigned pr = g; pr < n_pairs; pr += 16) {
+        const unsigned ra = 2 * pr, rb = 2 * pr + 1;
+        const bool has_b = rb < ring_num;
+        float2 x[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            float va = (polar[ra * kRingLen + l + 16 * m] - avg_f) * inv_f;
+            float vb = has_b ? (polar[rb * kRingLen + l + 16 * m] - avg_f) * inv_f : 0.f;
+            x[m] = make_float2(va, vb);
+        }
+        fft256_group<-1>(x, gws, tw, l, gmask);
+        // natural-order spectrum Z[l + 16 k2] to the workspace
+#pragma unroll
+        for (int k2 = 0; k2 < 16; k2++)
+            gws[l + 16 * k2] = x[k2];
+        __syncwarp(gmask);
+        // unpack the two real spectra and write slots k = l + 16 i (i = 0..7)
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int k = l + 16 * i;
+            float2 z = gws[k];
+            float2 zc = gws[(kRingLen - k) & (kRingLen - 1)];
+            // F_a = (Z[k] + conj Z[256-k]) / 2 ; F_b = (Z[k] - conj Z[256-k]) / (2i)
+            float2 fa = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y - zc.y));
+            float2 fb = make_float2(0.5f * (z.y + zc.y), -0.5f * (z.x - zc.x));
+            if (k == 0) {
+                // slot 0 carries (F[0], F[128]); both are real
+                float2 zn = gws[kSlots];
+                fa = make_float2(z.x, zn.x);
+                fb = make_float2(z.y, zn.y);
+            }
+            float wa = is_ref ? (float)(ra + 1) : 1.f;
+            float wb = is_ref ? (float)(rb + 1) : 1.f;
+            out_row[ra * kSlots + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
+            if (has_b)
+                out_row[rb * kSlots + k] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
+        }
+        __syncwarp(gmask);
+    }
+}
+
+cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
+                                 unsigned ring_num, const int2* shift_int, unsigned n_shift,
+                                 const float2* base, unsigned img0, unsigned n_img, int is_ref,
+                                 float2* out, cudaStream_t stream)
+{
+    if (n_img == 0 || n_shift == 0)
+        return cudaSuccess;
+    size_t smem = polar_spectra_smem_bytes(ring_num);
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(polar_spectra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)polar_spectra_smem_bytes(kMaxRingNum));
+        if (e != cudaSuccess)
+            return e;
+        configured = true;
+    }
+    unsigned rows = n_img * n_shift;
+    polar_spectra_kernel<<<rows, 256, smem, stream>>>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base,
+                                                       img0, n_img, is_ref, out);
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+} // namespace gpuisac

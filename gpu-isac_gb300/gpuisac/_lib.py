@@ -1,0 +1,125 @@
+"""ctypes binding of libgpu_aln_pack.so.
+
+The structures and argtypes are the ones the reference's drivers declare
+(bin/sp_isac2_gpu.py:121-187, bin/sp_isac_applications.py:86-157), so code
+written against the reference's gpu_aln_pack.so binds this library unchanged.
+There is no fallback: if the library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgpu_aln_pack.so")
+
+
+class AlignConfig(ctypes.Structure):
+    """Mirror of AlignConfig (cuda/gpu_aln_common.h:62-76)."""
+    _fields_ = [("sbj_num", ctypes.c_uint), ("ref_num", ctypes.c_uint), ("img_dim", ctypes.c_uint),
+                ("ring_num", ctypes.c_uint), ("ring_len", ctypes.c_uint),
+                ("shift_step", ctypes.c_float), ("shift_rng_x", ctypes.c_float),
+                ("shift_rng_y", ctypes.c_float), ("aln_type", ctypes.c_char_p)]
+
+
+class AlignParam(ctypes.Structure):
+    """Mirror of AlignParam (cuda/gpu_aln_common.h:78-85)."""
+    _fields_ = [("sbj_id", ctypes.c_int), ("ref_id", ctypes.c_int), ("shift_x", ctypes.c_float),
+                ("shift_y", ctypes.c_float), ("angle", ctypes.c_float), ("mirror", ctypes.c_bool)]
+
+
+aln_cfg_ptr = ctypes.POINTER(AlignConfig)
+aln_param_ptr = ctypes.POINTER(AlignParam)
+float_ptr = ctypes.POINTER(ctypes.c_float)
+float_ptr_ptr = ctypes.POINTER(float_ptr)
+
+# every symbol include/gpu_aln_pack.h declares
+EXPORTS = (
+    "multi_ref_align_init", "multi_ref_align", "gpu_clear", "reset_shifts", "print_gpu_info",
+    "get_texture_limit", "pre_align_init", "pre_align_size_check", "pre_align_fetch", "pre_align_run",
+    "ref_free_alignment_2D_init", "ref_free_alignment_2D_size_check", "ref_free_alignment_2D",
+    "ref_free_alignment_2D_filter_references", "gpuisac_last_error", "gpuisac_clear_error",
+    "gpuisac_version", "gpuisac_multi_ref_align_device", "gpuisac_spectra_device", "gpuisac_spectra_device_layout",
+    "gpuisac_ccf_peak_device", "gpuisac_shift_count", "gpuisac_launch_count", "gpuisac_profile",
+    "gpuisac_kernel_time",
+)
+
+
+class GpuIsacError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load the library (once) and declare its argtypes."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise GpuIsacError(f"{p} is missing: build it with gpu-isac_gb300/build.py")
+    L = ctypes.CDLL(p)
+    # the reference's own declarations (bin/sp_isac2_gpu.py:183-187)
+    L.multi_ref_align_init.argtypes = [aln_cfg_ptr, ctypes.c_uint]
+    L.multi_ref_align_init.restype = aln_param_ptr
+    L.multi_ref_align.argtypes = [float_ptr_ptr, float_ptr_ptr, float_ptr, float_ptr, ctypes.c_uint, ctypes.c_float]
+    L.multi_ref_align.restype = None
+    L.gpu_clear.argtypes = []
+    L.gpu_clear.restype = None
+    L.reset_shifts.argtypes = [ctypes.c_float, ctypes.c_float]
+    L.print_gpu_info.argtypes = [ctypes.c_uint]
+    L.get_texture_limit.argtypes = [ctypes.c_uint]
+    L.get_texture_limit.restype = ctypes.c_int
+    L.pre_align_init.restype = ctypes.c_ulonglong
+    L.ref_free_alignment_2D_init.restype = ctypes.c_ulonglong
+    L.pre_align_size_check.restype = ctypes.c_bool
+    L.ref_free_alignment_2D_size_check.restype = ctypes.c_bool
+    # additions
+    L.gpuisac_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.gpuisac_last_error.restype = ctypes.c_int
+    L.gpuisac_clear_error.argtypes = []
+    L.gpuisac_version.restype = ctypes.c_char_p
+    L.gpuisac_multi_ref_align_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.gpuisac_multi_ref_align_device.restype = ctypes.c_int
+    L.gpuisac_spectra_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.gpuisac_spectra_device.restype = ctypes.c_int
+    L.gpuisac_spectra_device_layout.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p,
+                                                ctypes.c_void_p]
+    L.gpuisac_spectra_device_layout.restype = ctypes.c_int
+    L.gpuisac_ccf_peak_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]
+    L.gpuisac_ccf_peak_device.restype = ctypes.c_int
+    L.gpuisac_launch_count.argtypes = []
+    L.gpuisac_launch_count.restype = ctypes.c_ulonglong
+    L.gpuisac_profile.argtypes = [ctypes.c_int]
+    L.gpuisac_kernel_time.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_ulonglong),
+                                      ctypes.POINTER(ctypes.c_double)]
+    L.gpuisac_kernel_time.restype = ctypes.c_int
+    L.gpuisac_shift_count.argtypes = [aln_cfg_ptr]
+    L.gpuisac_shift_count.restype = ctypes.c_int
+    if path is None:
+        _lib = L
+    return L
+
+
+def last_error(lib: ctypes.CDLL | None = None) -> tuple[int, str]:
+    L = lib or load()
+    buf = ctypes.create_string_buffer(512)
+    code = L.gpuisac_last_error(buf, 512)
+    return code, buf.value.decode(errors="replace")
+
+
+def check(lib: ctypes.CDLL | None = None) -> None:
+    """Raise GpuIsacError if the library recorded an error (and clear it)."""
+    L = lib or load()
+    code, msg = last_error(L)
+    if code:
+        L.gpuisac_clear_error()
+        raise GpuIsacError(f"gpuisac error {code}: {msg}")

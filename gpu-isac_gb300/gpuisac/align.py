@@ -1,0 +1,131 @@
+"""Python host side of the multi-reference alignment, mirroring the calls
+bin/sp_isac2_gpu.py:937-1032 makes (init, fill base shifts, align, clear),
+on numpy arrays or torch tensors instead of EMData lists.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import AlignConfig, GpuIsacError, float_ptr
+
+
+def make_config(sbj_num, ref_num, img_dim, ring_num, ring_len=256, shift_step=1.0, shift_rng_x=1.0,
+                shift_rng_y=1.0, aln_type=b"mref_aln") -> AlignConfig:
+    return AlignConfig(sbj_num, ref_num, img_dim, ring_num, ring_len, shift_step, shift_rng_x, shift_rng_y,
+                       aln_type)
+
+
+def ptr_array(stack: np.ndarray):
+    """float** over the images of a C-contiguous float32 [n][D][D] stack (the
+    reference's get_c_ptr_array, bin/sp_isac2_gpu.py:166-174)."""
+    assert stack.flags["C_CONTIGUOUS"] and stack.dtype == np.float32
+    n = stack.shape[0]
+    step = stack.strides[0]
+    base = stack.ctypes.data
+    arr = (float_ptr * max(n, 1))()
+    for i in range(n):
+        arr[i] = ctypes.cast(base + i * step, float_ptr)
+    return arr
+
+
+def multi_ref_align(particles: np.ndarray, refs: np.ndarray, ring_num: int, shift_rng_x: float,
+                    shift_rng_y: float, shift_step: float = 1.0, base_shifts: np.ndarray | None = None,
+                    ring_len: int = 256, device: int = 0, mem_request: float = 0.9, d_pitch: int | None = None):
+    """Align every particle against every reference through the C-ABI.
+
+    Returns (peak_list, d): peak_list [ref][4*sbj] float32 laid out as the
+    reference's caller expects (angle, sx, sy, mirror per particle), d
+    [ref][sbj] float32 peak correlations.
+    """
+    L = _lib.load()
+    particles = np.ascontiguousarray(particles, np.float32)
+    refs = np.ascontiguousarray(refs, np.float32)
+    P, D = particles.shape[0], particles.shape[1]
+    R = refs.shape[0]
+    if particles.shape[1:] != (D, D) or refs.shape[1:] != (D, D):
+        raise ValueError("particles and refs must be [n][D][D] with the same D")
+    cfg = make_config(P, R, D, ring_num, ring_len, shift_step, shift_rng_x, shift_rng_y)
+    pitch = d_pitch or P
+    peak_list = np.zeros((R, 4 * P), np.float32)
+    d = np.zeros((R, pitch), np.float32)
+    params = L.multi_ref_align_init(ctypes.byref(cfg), device)
+    if not params:
+        _lib.check(L)
+        raise GpuIsacError("multi_ref_align_init returned NULL")
+    try:
+        if base_shifts is not None:
+            bs = np.asarray(base_shifts, np.float32).reshape(P, 2)
+            for i in range(P):
+                params[i].shift_x = float(bs[i, 0])
+                params[i].shift_y = float(bs[i, 1])
+        sp, rp = ptr_array(particles), ptr_array(refs)
+        L.multi_ref_align(sp, rp, peak_list.ctypes.data_as(float_ptr), d.ctypes.data_as(float_ptr), pitch,
+                          mem_request)
+        _lib.check(L)
+    finally:
+        L.gpu_clear()
+    return peak_list, d[:, :P]
+
+
+def multi_ref_align_device(particles, refs, ring_num: int, shift_rng_x: float, shift_rng_y: float,
+                           shift_step: float = 1.0, base_shifts=None, stream=None, d_out=None, peak_out=None):
+    """Device-resident form on torch CUDA tensors: returns (d [R][P], peak [R][P][4])."""
+    import torch
+
+    if not (particles.is_cuda and refs.is_cuda):
+        raise GpuIsacError("multi_ref_align_device needs CUDA tensors")
+    particles = particles.contiguous().float()
+    refs = refs.contiguous().float()
+    P, D = particles.shape[0], particles.shape[1]
+    R = refs.shape[0]
+    cfg = make_config(P, R, D, ring_num, 256, shift_step, shift_rng_x, shift_rng_y)
+    if d_out is None:
+        d_out = torch.empty((R, P), dtype=torch.float32, device=particles.device)
+    if peak_out is None:
+        peak_out = torch.empty((R, P, 4), dtype=torch.float32, device=particles.device)
+    base_ptr = None
+    if base_shifts is not None:
+        base_shifts = base_shifts.contiguous().float()
+        base_ptr = base_shifts.data_ptr()
+    st = stream if stream is not None else torch.cuda.current_stream(particles.device)
+    L = _lib.load()
+    rc = L.gpuisac_multi_ref_align_device(ctypes.byref(cfg), particles.data_ptr(), refs.data_ptr(), base_ptr,
+                                          d_out.data_ptr(), peak_out.data_ptr(), st.cuda_stream)
+    if rc:
+        _lib.check(L)
+        raise GpuIsacError(f"gpuisac_multi_ref_align_device failed ({rc})")
+    return d_out, peak_out
+
+
+def spectra_device(imgs, ring_num: int, shift_rng_x: float, shift_rng_y: float, shift_step: float = 1.0,
+                   is_ref: bool = False, base_shifts=None, sbj_num: int | None = None):
+    """Ring spectra of a device image stack as the CCF kernel consumes them:
+    [n][n_shift][ring][128][2] float32 (n_shift = 1 for references)."""
+    import torch
+
+    imgs = imgs.contiguous().float()
+    n, D = imgs.shape[0], imgs.shape[1]
+    cfg = make_config(sbj_num or n, n if is_ref else 1, D, ring_num, 256, shift_step, shift_rng_x, shift_rng_y)
+    L = _lib.load()
+    S = 1 if is_ref else L.gpuisac_shift_count(ctypes.byref(cfg))
+    out = torch.empty((n, S, ring_num, 128, 2), dtype=torch.float32, device=imgs.device)
+    base_ptr = None
+    if base_shifts is not None:
+        base_shifts = base_shifts.contiguous().float()
+        base_ptr = base_shifts.data_ptr()
+    st = torch.cuda.current_stream(imgs.device)
+    rc = L.gpuisac_spectra_device(ctypes.byref(cfg), imgs.data_ptr(), n, int(is_ref), base_ptr, out.data_ptr(),
+                                  st.cuda_stream)
+    if rc:
+        _lib.check(L)
+        raise GpuIsacError(f"gpuisac_spectra_device failed ({rc})")
+    return out
+
+
+def peak_tuples(peak_list: np.ndarray) -> np.ndarray:
+    """[ref][4*sbj] -> [ref][sbj][4]"""
+    R = peak_list.shape[0]
+    return peak_list.reshape(R, -1, 4)

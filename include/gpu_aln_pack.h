@@ -1,0 +1,166 @@
+/*
+ * gpu_aln_pack.h -- C-ABI of the GB300 multi-reference alignment library
+ * (libgpu_aln_pack.so, a drop-in for the reference's gpu_aln_pack.so).
+ *
+ * Every declaration below names the reference interface it replaces
+ * (paths inside the GPU-ISAC repository).  Types are plain C: no CUDA or
+ * PyTorch types cross this boundary.  Callers bind it with ctypes exactly as
+ * bin/sp_isac2_gpu.py:121-187 and bin/sp_isac_applications.py:86-157 do.
+ */
+#ifndef GPU_ALN_PACK_H
+#define GPU_ALN_PACK_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Replaces struct AlignConfig, cuda/gpu_aln_common.h:62-76 (40 bytes on LP64;
+ * the pointer is stored, not copied, so the struct must outlive the calls).
+ * Python mirror: bin/sp_isac2_gpu.py:139-152. */
+typedef struct AlignConfig {
+    unsigned int sbj_num;
+    unsigned int ref_num;
+    unsigned int img_dim;
+    unsigned int ring_num;
+    unsigned int ring_len;
+    float shift_step;
+    float shift_rng_x;
+    float shift_rng_y;
+    const char *aln_type; /* "mref_aln" for the multi-reference path */
+} AlignConfig;
+
+/* Replaces struct AlignParam, cuda/gpu_aln_common.h:78-85 (24 bytes).
+ * Python mirror: bin/sp_isac2_gpu.py:154-160.  The multi-reference path reads
+ * shift_x / shift_y as each particle's base shift. */
+typedef struct AlignParam {
+    int sbj_id;
+    int ref_id;
+    float shift_x;
+    float shift_y;
+    float angle;
+    bool mirror;
+} AlignParam;
+
+/* ---- multi-reference alignment (the hot path) ---- */
+
+/* Replaces multi_ref_align_init, cuda/gpu_aln_noref.h:61-64 /
+ * cuda/gpu_aln_noref.cu:311-324.  Selects the device, builds the polar
+ * template and shift grid, and returns a zero-filled, host-writable
+ * AlignParam[sbj_num] owned by the library (freed by gpu_clear).
+ * Returns NULL on error (see gpuisac_last_error). */
+AlignParam *multi_ref_align_init(const AlignConfig *aln_cfg, unsigned int cuda_device_id);
+
+/* Replaces multi_ref_align, cuda/gpu_aln_noref.h:66-73 /
+ * cuda/gpu_aln_noref.cu:326-554.  sbj_data: sbj_num pointers to img_dim^2
+ * float images (row-major); ref_data: ref_num pointers.  Writes
+ * isac_peak_list[(q*sbj_num + p)*4 + {0..3}] = (angle, shift_x, shift_y,
+ * mirror) and isac_d[q*isac_d_pitch + p] = the peak correlation, for every
+ * reference q and particle p.  cuda_mem_request: fraction of free device
+ * memory the call may use for its work space. */
+void multi_ref_align(const float **sbj_data, const float **ref_data, float *isac_peak_list, float *isac_d,
+                     unsigned int isac_d_pitch, float cuda_mem_request);
+
+/* Replaces gpu_clear, cuda/gpu_aln_noref.h:57 / cuda/gpu_aln_noref.cu:139-180. */
+void gpu_clear(void);
+
+/* Replaces reset_shifts, cuda/gpu_aln_noref.cu:117-137: rebuilds the shift
+ * grid with range (shift_range, shift_range); the number of shifts must not
+ * change. */
+void reset_shifts(float shift_range, float shift_step);
+
+/* Replaces print_gpu_info, cuda/gpu_aln_common.h:124 / gpu_aln_common.cu:180-218. */
+void print_gpu_info(unsigned int device_idx);
+
+/* Replaces get_texture_limit, cuda/gpu_aln_common.h:133 / gpu_aln_common.cu:233-237:
+ * images of side img_dim that fit the height of one 2D linear texture. */
+int get_texture_limit(unsigned int img_dim);
+
+/* ---- adjacent paths bound by the callers (present so that ctypes binding
+ * succeeds; not built in this library: each records an error and returns a
+ * failure value) ---- */
+
+/* Replaces pre_align_init, cuda/gpu_aln_noref.h:77-81. */
+AlignParam *pre_align_init(unsigned int num_particles, const AlignConfig *aln_cfg, unsigned int cuda_device_id);
+/* Replaces pre_align_size_check, cuda/gpu_aln_noref.h:83-89. */
+bool pre_align_size_check(unsigned int num_particles, const AlignConfig *cfg, unsigned int cuda_device_id,
+                          float request, bool verbose);
+/* Replaces pre_align_fetch, cuda/gpu_aln_noref.h:91-95. */
+void pre_align_fetch(const float **img_data, unsigned int img_num, const char *batch_type);
+/* Replaces pre_align_run, cuda/gpu_aln_noref.h:97. */
+void pre_align_run(int start_idx, int stop_idx);
+/* Replaces ref_free_alignment_2D_init, cuda/gpu_aln_noref.h:101-107. */
+AlignParam *ref_free_alignment_2D_init(const AlignConfig *aln_cfg, const float **sbj_data_list,
+                                       const float **ref_data_list, const int *sbj_cid_list,
+                                       unsigned int cuda_device_id);
+/* Replaces ref_free_alignment_2D_size_check, cuda/gpu_aln_noref.h:109-114. */
+bool ref_free_alignment_2D_size_check(const AlignConfig *cfg, unsigned int cuda_device_id, float request,
+                                      bool verbose);
+/* Replaces ref_free_alignment_2D, cuda/gpu_aln_noref.h:116. */
+void ref_free_alignment_2D(void);
+/* Replaces ref_free_alignment_2D_filter_references, cuda/gpu_aln_noref.h:118. */
+void ref_free_alignment_2D_filter_references(float cutoff_freq, float falloff);
+
+/* ---- additions of this library (no counterpart in the reference, which
+ * prints and exits on any CUDA error, cuda/gpu_aln_common.cu:104-118) ---- */
+
+/* Last error of the calling process: returns its code (0 = none) and copies
+ * the message into buf (NUL-terminated, truncated to n bytes). */
+int gpuisac_last_error(char *buf, size_t n);
+/* Clears the recorded error. */
+void gpuisac_clear_error(void);
+/* Library version, e.g. "gpuisac-gb300 0.1.0". */
+const char *gpuisac_version(void);
+
+/* Device-resident form of multi_ref_align for callers that keep images in
+ * GPU memory (all pointers are device pointers on the current device):
+ * sbj [sbj_num][img_dim][img_dim], ref [ref_num][img_dim][img_dim],
+ * base_shift [sbj_num][2] or NULL, d_out [ref_num][sbj_num],
+ * peak_out [ref_num][sbj_num][4].  stream: a cudaStream_t or NULL.
+ * Blocks until the results are written.  Returns 0 or an error code. */
+int gpuisac_multi_ref_align_device(const AlignConfig *cfg, const float *sbj, const float *ref,
+                                   const float *base_shift, float *d_out, float *peak_out, void *stream);
+
+/* Ring spectra of a device image stack at every shift of cfg's grid, as the
+ * CCF kernel consumes them: out [n_img][n_shift][ring_num][128][2] (float),
+ * slot 0 = (F[0], F[128]); is_ref selects the reference layout (ring weight
+ * folded in, no shift).  base_shift may be NULL.  For tests and diagnostics. */
+int gpuisac_spectra_device(const AlignConfig *cfg, const float *imgs, unsigned int n_img, int is_ref,
+                           const float *base_shift, float *out, void *stream);
+
+/* Same, with an explicit image grouping: images are read as the reference's
+ * textures read them, in batches of `batch` images split into textures of
+ * `tex` images.  For tests. */
+int gpuisac_spectra_device_layout(const AlignConfig *cfg, const float *imgs, unsigned int n_img, int is_ref,
+                                  const float *base_shift, unsigned int batch, unsigned int tex, float *out,
+                                  void *stream);
+
+/* The CCF / inverse FFT / peak-search stage alone, on spectra made by
+ * gpuisac_spectra_device: sbj_spectra holds n_part particles (global indices
+ * p_global0..), ref_spectra cfg->ref_num references; writes their columns of
+ * d_out [ref_num][sbj_num] and peak_out [ref_num][sbj_num][4].  Asynchronous
+ * on `stream`.  Returns 0 or an error code. */
+int gpuisac_ccf_peak_device(const AlignConfig *cfg, const float *sbj_spectra, const float *ref_spectra,
+                            const float *base_shift, unsigned int n_part, unsigned int p_global0, float *d_out,
+                            float *peak_out, void *stream);
+
+/* Number of shifts in cfg's grid (the reference's generate_shift_array). */
+int gpuisac_shift_count(const AlignConfig *cfg);
+
+/* Kernels this library has launched since it was loaded. */
+unsigned long long gpuisac_launch_count(void);
+
+/* Turns CUDA-event timing of each pipeline kernel on (1) or off (0) and
+ * resets the totals. */
+void gpuisac_profile(int on);
+
+/* Launches and summed device time (ms) of one pipeline kernel
+ * ("polar_spectra" or "ccf_peak") since gpuisac_profile(1). */
+int gpuisac_kernel_time(const char *kernel, unsigned long long *launches, double *total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,192 @@
+"""ctypes front-end of the CPU oracle (oracle/_build/libisac_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference legs, never by the product path.  The C
+sources restate the reference's GPU path; see isac_oracle.h for the
+file:line map.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libisac_oracle.so")
+_lib = None
+
+
+class OrcCfg(ctypes.Structure):
+    _fields_ = [("sbj_num", ctypes.c_uint), ("ref_num", ctypes.c_uint),
+                ("img_dim", ctypes.c_uint), ("ring_num", ctypes.c_uint),
+                ("ring_len", ctypes.c_uint), ("shift_step", ctypes.c_float),
+                ("shift_rng_x", ctypes.c_float), ("shift_rng_y", ctypes.c_float)]
+
+
+class OrcLayout(ctypes.Structure):
+    _fields_ = [("sbj_batch", ctypes.c_uint), ("tex_limit", ctypes.c_uint),
+                ("ref_batch", ctypes.c_uint)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc, OpenMP)."""
+    if force or not os.path.exists(_LIB_PATH) or _stale():
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def _stale() -> bool:
+    t = os.path.getmtime(_LIB_PATH)
+    return any(os.path.getmtime(os.path.join(_HERE, f)) > t
+               for f in ("isac_oracle.c", "isac_oracle.h", "isac_oracle_core.h"))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        fp = ctypes.POINTER(ctypes.c_float)
+        dp = ctypes.POINTER(ctypes.c_double)
+        cfgp = ctypes.POINTER(OrcCfg)
+        layp = ctypes.POINTER(OrcLayout)
+        L.orc_polar_template.argtypes = [ctypes.c_uint, ctypes.c_uint, fp]
+        L.orc_shift_array.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int]
+        L.orc_shift_array.restype = ctypes.c_int
+        L.orc_tex_split.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_int), fp]
+        L.orc_reference_sbj_batch.argtypes = [cfgp]
+        L.orc_reference_sbj_batch.restype = ctypes.c_uint
+        for pfx, rp in (("f64", dp), ("f32", fp)):
+            f = getattr(L, f"orc_{pfx}_polar")
+            f.argtypes = [cfgp, layp, fp, ctypes.c_uint, ctypes.c_uint, ctypes.c_int,
+                          ctypes.c_float, ctypes.c_float, fp, rp]
+            f = getattr(L, f"orc_{pfx}_spectra")
+            f.argtypes = [cfgp, layp, fp, ctypes.c_uint, ctypes.c_uint, ctypes.c_int,
+                          ctypes.c_float, ctypes.c_float, fp, rp]
+            f = getattr(L, f"orc_{pfx}_pair_ccf")
+            f.argtypes = [cfgp, layp, fp, fp, ctypes.c_uint, ctypes.c_uint, fp, rp]
+            f = getattr(L, f"orc_{pfx}_multi_ref_align")
+            f.argtypes = [cfgp, layp, fp, fp, fp, fp, rp, ctypes.c_uint, ctypes.c_int]
+        L.orc_f64_peak_search.argtypes = [dp, ctypes.c_uint, ctypes.c_uint, fp, dp,
+                                          ctypes.POINTER(ctypes.c_uint)]
+        _lib = L
+    return _lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_cfg(sbj_num, ref_num, img_dim, ring_num, ring_len=256, shift_step=1.0,
+             shift_rng_x=1.0, shift_rng_y=1.0) -> OrcCfg:
+    return OrcCfg(sbj_num, ref_num, img_dim, ring_num, ring_len, shift_step, shift_rng_x, shift_rng_y)
+
+
+def reference_layout(cfg: OrcCfg, tex_height: int = 65000) -> OrcLayout:
+    """Image grouping the reference uses on a device whose
+    maxTexture2DLinear height is tex_height (65000 on current GPUs)."""
+    sb = lib().orc_reference_sbj_batch(ctypes.byref(cfg))
+    return OrcLayout(max(sb, 1), max(tex_height // cfg.img_dim, 1), max(min(cfg.ref_num, 100), 1))
+
+
+def polar_template(ring_num: int, ring_len: int) -> np.ndarray:
+    out = np.zeros((ring_num, ring_len, 2), np.float32)
+    lib().orc_polar_template(ring_num, ring_len, _fp(out))
+    return out
+
+
+def shift_array(rx: float, ry: float, step: float) -> np.ndarray:
+    cap = 1 << 16
+    out = np.zeros((cap, 2), np.float32)
+    n = lib().orc_shift_array(rx, ry, step, _fp(out), cap)
+    if n < 0:
+        raise ValueError("bad shift grid")
+    return out[:n].copy()
+
+
+def tex_split(t: float):
+    i = ctypes.c_int()
+    a = ctypes.c_float()
+    lib().orc_tex_split(t, ctypes.byref(i), ctypes.byref(a))
+    return i.value, a.value
+
+
+def _real(precision):
+    return (np.float64, _dp) if precision == "f64" else (np.float32, _fp)
+
+
+def polar(cfg, lay, stack, img, is_ref=False, shift=(0.0, 0.0), base=None, precision="f64"):
+    dt, cast = _real(precision)
+    stack = np.ascontiguousarray(stack, np.float32)
+    out = np.zeros((cfg.ring_num, cfg.ring_len), dt)
+    b = None if base is None else np.ascontiguousarray(base, np.float32)
+    rc = getattr(lib(), f"orc_{precision}_polar")(
+        ctypes.byref(cfg), ctypes.byref(lay), _fp(stack), stack.shape[0], img, int(is_ref),
+        shift[0], shift[1], None if b is None else _fp(b), cast(out))
+    if rc:
+        raise RuntimeError("oracle polar failed")
+    return out
+
+
+def spectra(cfg, lay, stack, img, is_ref=False, shift=(0.0, 0.0), base=None, precision="f64"):
+    dt, cast = _real(precision)
+    stack = np.ascontiguousarray(stack, np.float32)
+    out = np.zeros((cfg.ring_num, cfg.ring_len // 2 + 1, 2), dt)
+    b = None if base is None else np.ascontiguousarray(base, np.float32)
+    rc = getattr(lib(), f"orc_{precision}_spectra")(
+        ctypes.byref(cfg), ctypes.byref(lay), _fp(stack), stack.shape[0], img, int(is_ref),
+        shift[0], shift[1], None if b is None else _fp(b), cast(out))
+    if rc:
+        raise RuntimeError("oracle spectra failed")
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def pair_ccf(cfg, lay, sbj, ref, p, q, base_shifts=None, precision="f64"):
+    """c[mirror][shift][tau] of one particle/reference pair."""
+    dt, cast = _real(precision)
+    n_shift = len(shift_array(cfg.shift_rng_x, cfg.shift_rng_y, cfg.shift_step))
+    out = np.zeros((2, n_shift, cfg.ring_len), dt)
+    sbj = np.ascontiguousarray(sbj, np.float32)
+    ref = np.ascontiguousarray(ref, np.float32)
+    b = None if base_shifts is None else np.ascontiguousarray(base_shifts, np.float32)
+    rc = getattr(lib(), f"orc_{precision}_pair_ccf")(
+        ctypes.byref(cfg), ctypes.byref(lay), _fp(sbj), _fp(ref), p, q,
+        None if b is None else _fp(b), cast(out))
+    if rc:
+        raise RuntimeError("oracle pair_ccf failed")
+    return out
+
+
+def multi_ref_align(cfg, lay, sbj, ref, base_shifts=None, precision="f64", threads=0):
+    """Returns (peak_list [R][P][4] float32, d [R][P])."""
+    dt, cast = _real(precision)
+    P, R = cfg.sbj_num, cfg.ref_num
+    sbj = np.ascontiguousarray(sbj, np.float32)
+    ref = np.ascontiguousarray(ref, np.float32)
+    assert sbj.shape[0] == P and ref.shape[0] == R
+    peak = np.zeros((R, P, 4), np.float32)
+    d = np.zeros((R, P), dt)
+    b = None if base_shifts is None else np.ascontiguousarray(base_shifts, np.float32)
+    rc = getattr(lib(), f"orc_{precision}_multi_ref_align")(
+        ctypes.byref(cfg), ctypes.byref(lay), _fp(sbj), _fp(ref),
+        None if b is None else _fp(b), _fp(peak), cast(d), P, threads)
+    if rc:
+        raise RuntimeError("oracle multi_ref_align failed")
+    return peak, d
+
+
+def peak_search(ccf: np.ndarray):
+    """First-strict-max search + parabola on ccf [2*S][L] (FP64)."""
+    ccf = np.ascontiguousarray(ccf, np.float64)
+    two_s, L = ccf.shape
+    out = np.zeros(4, np.float32)
+    pk = ctypes.c_double()
+    tau = ctypes.c_uint()
+    lib().orc_f64_peak_search(_dp(ccf), two_s // 2, L, _fp(out), ctypes.byref(pk), ctypes.byref(tau))
+    return out, pk.value, tau.value

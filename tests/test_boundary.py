@@ -1,0 +1,116 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every symbol
+include/gpu_aln_pack.h declares, its structs match the reference's ctypes
+mirrors byte for byte, and argument errors are reported, not fatal."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gpu_aln_pack.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gpuisac_build", os.path.join(ROOT, "gpu-isac_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build()
+    from gpuisac import _lib
+    return _lib.load()
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", src)
+    skip = {"if", "defined", "sizeof"}
+    return sorted({n for n in names if n not in skip})
+
+
+def test_header_declares_the_reference_exports():
+    names = set(declared_functions())
+    for ref_export in ("multi_ref_align_init", "multi_ref_align", "gpu_clear", "reset_shifts", "print_gpu_info",
+                       "get_texture_limit", "pre_align_init", "pre_align_size_check", "pre_align_fetch",
+                       "pre_align_run", "ref_free_alignment_2D_init", "ref_free_alignment_2D_size_check",
+                       "ref_free_alignment_2D", "ref_free_alignment_2D_filter_references"):
+        assert ref_export in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    so = os.path.join(ROOT, "gpu-isac_gb300", "lib", "libgpu_aln_pack.so")
+    out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    from gpuisac import _lib
+    assert set(_lib.EXPORTS) == set(declared_functions())
+    for n in declared_functions():
+        getattr(lib, n)
+
+
+def test_dropin_file_name_exists(lib):
+    assert os.path.exists(os.path.join(ROOT, "gpu-isac_gb300", "lib", "gpu_aln_pack.so"))
+
+
+def test_struct_layout_matches_reference():
+    from gpuisac import AlignConfig, AlignParam
+    # cuda/gpu_aln_common.h:62-85 on LP64
+    assert ctypes.sizeof(AlignConfig) == 40 and AlignConfig.aln_type.offset == 32
+    assert ctypes.sizeof(AlignParam) == 24 and AlignParam.mirror.offset == 20
+
+
+def _cfg(**kw):
+    from gpuisac import make_config
+    base = dict(sbj_num=10, ref_num=3, img_dim=64, ring_num=29, ring_len=256, shift_step=1.0, shift_rng_x=2.0,
+                shift_rng_y=2.0)
+    base.update(kw)
+    return make_config(**base)
+
+
+def test_shift_count_host_only(lib):
+    assert lib.gpuisac_shift_count(ctypes.byref(_cfg())) == 25
+    assert lib.gpuisac_shift_count(ctypes.byref(_cfg(shift_rng_x=3.0, shift_rng_y=3.0))) == 49
+    assert lib.gpuisac_shift_count(ctypes.byref(_cfg(shift_rng_x=0.0, shift_rng_y=0.0))) == 1
+
+
+@pytest.mark.parametrize("kw,code", [(dict(ring_len=128), 4), (dict(ring_num=0), 4), (dict(ring_num=500), 4),
+                                     (dict(img_dim=1), 2), (dict(shift_step=0.0), 2),
+                                     (dict(aln_type=b"pre_aln"), 4)])
+def test_init_rejects_bad_config(lib, kw, code):
+    from gpuisac import _lib
+    cfg = _cfg(**kw)
+    lib.gpuisac_clear_error()
+    p = lib.multi_ref_align_init(ctypes.byref(cfg), 0)
+    assert not p
+    c, msg = _lib.last_error(lib)
+    assert c == code and msg
+    lib.gpuisac_clear_error()
+    assert _lib.last_error(lib)[0] == 0
+
+
+def test_align_before_init_is_an_error(lib):
+    from gpuisac import _lib
+    lib.gpu_clear()
+    lib.gpuisac_clear_error()
+    lib.multi_ref_align(None, None, None, None, 10, ctypes.c_float(0.9))
+    assert _lib.last_error(lib)[0] == 3
+    lib.gpuisac_clear_error()
+
+
+def test_adjacent_paths_fail_loudly(lib):
+    from gpuisac import _lib
+    lib.gpuisac_clear_error()
+    assert lib.pre_align_init(10, ctypes.byref(_cfg(aln_type=b"pre_aln")), 0) == 0
+    code, msg = _lib.last_error(lib)
+    assert code == 4 and "multi-reference" in msg
+    lib.gpuisac_clear_error()
+
+
+def test_python_host_raises_without_library(tmp_path):
+    from gpuisac import _lib
+    with pytest.raises(_lib.GpuIsacError):
+        _lib.load(str(tmp_path / "missing.so"))

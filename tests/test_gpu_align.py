@@ -1,0 +1,129 @@
+"""The whole multi-reference alignment on the GPU, through the C-ABI, against
+the FP64 oracle.
+
+Parity bar (floating point): peak values within 1e-4 relative of the FP64
+oracle; the same best (ref, angle, sx, sy, mirror) for >= 99.5% of particles
+(angle compared circularly within ANGLE_TOL degrees).
+"""
+import numpy as np
+import pytest
+
+from gpuisac import synth
+
+pytestmark = pytest.mark.gpu
+
+PEAK_RTOL = 1e-4
+ANGLE_TOL = 0.05
+SAME_BEST = 0.995
+SAME_PAIR = 0.99
+
+
+def circ_diff(a, b):
+    d = (np.asarray(a, np.float64) - np.asarray(b, np.float64)) % 360.0
+    return np.minimum(d, 360.0 - d)
+
+
+def compare(peak_g, d_g, peak_o, d_o):
+    """peak_* [R][P][4], d_* [R][P]"""
+    rel = np.abs(d_g.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), 1e-30)
+    assert rel.max() <= PEAK_RTOL, rel.max()
+    same_tuple = (peak_g[..., 1:] == peak_o[..., 1:]).all(-1) & (circ_diff(peak_g[..., 0], peak_o[..., 0]) < ANGLE_TOL)
+    qg, qo = np.argmax(d_g, 0), np.argmax(d_o, 0)
+    P = d_o.shape[1]
+    best_same = (qg == qo) & same_tuple[qo, np.arange(P)]
+    assert best_same.mean() >= SAME_BEST, best_same.mean()
+    assert same_tuple.mean() >= SAME_PAIR, same_tuple.mean()
+    return rel.max(), best_same.mean(), same_tuple.mean()
+
+
+def oracle_run(oracle_mod, parts, refs, NR, rng, base=None, tex=None):
+    import oracle
+    P, D = parts.shape[0], parts.shape[1]
+    cfg = oracle.make_cfg(P, refs.shape[0], D, NR, 256, 1.0, rng, rng)
+    lay = oracle.reference_layout(cfg)
+    if tex is not None:
+        lay = oracle.OrcLayout(lay.sbj_batch, tex, lay.ref_batch)
+    return oracle_mod.multi_ref_align(cfg, lay, parts, refs, base_shifts=base)
+
+
+@pytest.fixture(scope="module")
+def small_case():
+    return synth.make_stack(120, 64, 12, 2, 0.1, 28.0, 31)
+
+
+def test_host_abi_matches_oracle(gpulib, cuda, oracle_mod, small_case):
+    from gpuisac import multi_ref_align
+    st = small_case
+    pl, d = multi_ref_align(st.particles, st.refs, 29, 2.0, 2.0)
+    peak_g = pl.reshape(12, 120, 4)
+    peak_o, d_o = oracle_run(oracle_mod, st.particles, st.refs, 29, 2.0, tex=gpulib.get_texture_limit(64))
+    compare(peak_g, d, peak_o, d_o)
+    # the synthetic ground truth comes back too
+    q = np.argmax(d, 0)
+    assert (q == st.cls).mean() > 0.95
+
+
+def test_d_pitch_leaves_other_columns(gpulib, cuda, small_case):
+    """isac_d points into a wider node-wide array (bin/sp_isac2_gpu.py:995):
+    only this call's columns are written."""
+    import ctypes
+
+    from gpuisac import _lib, make_config
+    from gpuisac.align import ptr_array
+    st = small_case
+    P, R, pitch = 120, 12, 173
+    cfg = make_config(P, R, 64, 29, 256, 1.0, 2.0, 2.0)
+    params = gpulib.multi_ref_align_init(ctypes.byref(cfg), 0)
+    assert params
+    d = np.full((R, pitch), -7.0, np.float32)
+    pl = np.zeros((R, 4 * P), np.float32)
+    gpulib.multi_ref_align(ptr_array(st.particles), ptr_array(st.refs), pl.ctypes.data_as(_lib.float_ptr),
+                           d.ctypes.data_as(_lib.float_ptr), pitch, ctypes.c_float(0.9))
+    _lib.check(gpulib)
+    gpulib.gpu_clear()
+    assert (d[:, P:] == -7.0).all() and (d[:, :P] != -7.0).all()
+
+
+def test_device_path_matches_host_path(gpulib, cuda, small_case):
+    import torch
+
+    from gpuisac import multi_ref_align, multi_ref_align_device
+    st = small_case
+    pl, d = multi_ref_align(st.particles, st.refs, 29, 2.0, 2.0)
+    dg, pg = multi_ref_align_device(torch.from_numpy(st.particles).to(cuda), torch.from_numpy(st.refs).to(cuda),
+                                    29, 2.0, 2.0)
+    assert np.array_equal(dg.cpu().numpy(), d)
+    assert np.array_equal(pg.cpu().numpy(), pl.reshape(12, 120, 4))
+
+
+def test_two_refs_per_cta_path_and_partial_tile(gpulib, cuda, oracle_mod):
+    """61 rings (more than one ring chunk, 2 references per CTA), 5 references
+    (a partial tile), large box, fractional base shifts."""
+    from gpuisac import multi_ref_align
+    st = synth.make_stack(16, 128, 5, 1, 0.05, 60.0, 32)
+    base = np.random.default_rng(1).uniform(-1.2, 1.2, (16, 2)).astype(np.float32)
+    pl, d = multi_ref_align(st.particles, st.refs, 61, 1.0, 1.0, base_shifts=base)
+    peak_o, d_o = oracle_run(oracle_mod, st.particles, st.refs, 61, 1.0, base=base,
+                             tex=gpulib.get_texture_limit(128))
+    compare(pl.reshape(5, 16, 4), d, peak_o, d_o)
+
+
+@pytest.mark.parametrize("P,R,D,NR,rng", [(1, 1, 64, 29, 2.0), (9, 3, 65, 30, 0.0), (7, 6, 48, 1, 1.0),
+                                          (33, 9, 76, 35, 3.0)])
+def test_edge_shapes(gpulib, cuda, oracle_mod, P, R, D, NR, rng):
+    from gpuisac import multi_ref_align
+    st = synth.make_stack(P, D, R, int(rng), 0.1, D * 0.4, 33 + P)
+    pl, d = multi_ref_align(st.particles, st.refs, NR, rng, rng)
+    peak_o, d_o = oracle_run(oracle_mod, st.particles, st.refs, NR, rng, tex=gpulib.get_texture_limit(D))
+    rel = np.abs(d.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), 1e-30)
+    assert rel.max() <= PEAK_RTOL
+    same = (pl.reshape(R, P, 4)[..., 1:] == peak_o[..., 1:]).all(-1)
+    assert same.mean() >= (1.0 if P * R < 50 else SAME_PAIR)
+
+
+def test_repeated_calls_are_identical(gpulib, cuda, small_case):
+    from gpuisac import multi_ref_align
+    st = small_case
+    a = multi_ref_align(st.particles[:40], st.refs, 29, 2.0, 2.0)
+    b = multi_ref_align(st.particles[:40], st.refs, 29, 2.0, 2.0)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
