@@ -167,10 +167,13 @@ __device__ __forceinline__ const float* tex_row(const StackDesc& s, const TexPla
 }
 
 // fixed-point split of a texel-space coordinate: 8 fractional bits, round to
-// nearest even (same rule as the oracle's orc_tex_split)
+// nearest with ties upward, as the texture unit does (same rule as the
+// oracle's orc_tex_split).  x = (t - 0.5) * 256 is exact in float.
 __device__ __forceinline__ void tex_split(float t, int& i, float& a)
 {
-    int q = __float2int_rn((t - 0.5f) * 256.0f);
+    const float x = (t - 0.5f) * 256.0f;
+    const float fl = floorf(x);
+    int q = (int)fl + ((x - fl) >= 0.5f ? 1 : 0);
     i = q >> 8;
     a = (float)(q & 255) * (1.0f / 256.0f);
 }

@@ -52,13 +52,13 @@ int orc_shift_array(float rng_x, float rng_y, float step, float *out_xy, int cap
 /* Texture unit, linear filter, unnormalised coordinates
  * (cuda/gpu_aln_noref.cu:2333-2336): the texel-space coordinate t is moved by
  * -0.5 and converted to fixed point with 8 fractional bits, rounding to
- * nearest; the integer part selects the left texel, the fraction is the
- * weight of the right one.  The rounding rule is pinned against the texture
- * unit by tests/test_gpu_texture.py. */
+ * nearest with ties upward; the integer part selects the left texel, the
+ * fraction is the weight of the right one.  The rounding rule is pinned
+ * against the texture unit by tests/test_gpu_texture.py. */
 void orc_tex_split(float t, int *i, float *a)
 {
     float tb = t - 0.5f;
-    double q = nearbyint((double)tb * 256.0);
+    double q = floor((double)tb * 256.0 + 0.5);
     double fi = floor(q / 256.0);
     *i = (int)fi;
     *a = (float)((q - fi * 256.0) / 256.0);

@@ -38,8 +38,9 @@ def test_shift_grid_order(oracle_mod):
 
 
 @pytest.mark.parametrize("t,expect", [(10.5, (10, 0.0)), (10.75, (10, 0.25)), (0.5, (0, 0.0)),
-                                      (0.0, (-1, 0.5)), (10.5 + 1.0 / 512, (10, 0.0)),
-                                      (10.5 + 3.0 / 512, (10, 2.0 / 256)), (11.49999, (11, 0.0))])
+                                      (0.0, (-1, 0.5)), (10.5 + 1.0 / 512, (10, 1.0 / 256)),
+                                      (10.5 + 3.0 / 512, (10, 2.0 / 256)), (11.49999, (11, 0.0)),
+                                      (10.5 + 511.0 / 512, (11, 0.0))])
 def test_texture_weight_rounding(oracle_mod, t, expect):
     i, a = oracle_mod.tex_split(t)
     assert (i, a) == expect
