@@ -20,6 +20,7 @@
 
 #include "../../include/gpu_aln_pack.h"
 #include "gpuisac_kernels.h"
+#include "host_geometry.h"
 
 using namespace gpuisac;
 
@@ -520,6 +521,33 @@ void clear_state(State& s)
 }
 
 } // namespace
+
+namespace gpuisac {
+
+int host_geometry(const AlignConfig* cfg, HostGeometry& out)
+{
+    Geometry g;
+    int rc = validate(cfg, g, false);
+    if (rc)
+        return rc;
+    out.P = g.P;
+    out.R = g.R;
+    out.D = g.D;
+    out.NR = g.NR;
+    out.S = g.S;
+    out.shifts_f = g.shifts_f;
+    out.shifts_i = g.shifts_i;
+    out.tmpl = g.tmpl;
+    out.tw = twiddles();
+    out.sbj_batch = std::max(1u, reference_sbj_batch(cfg));
+    return 0;
+}
+
+unsigned texture_images(int dev, unsigned dim) { return std::max(1u, texture_image_limit(dev, std::max(dim, 1u))); }
+
+void record_error(int code, const char* msg) { set_error(code, "%s", msg); }
+
+} // namespace gpuisac
 
 // ====================================================================== C-ABI
 extern "C" {

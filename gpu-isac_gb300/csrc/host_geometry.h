@@ -1,0 +1,32 @@
+// host_geometry.h -- host-side helpers of align_abi.cu shared with other
+// translation units of this library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/gpu_aln_pack.h"
+
+namespace gpuisac {
+
+struct HostGeometry {
+    unsigned P = 0, R = 0, D = 0, NR = 0, S = 0;
+    std::vector<float2> shifts_f; // the reference's float shift grid
+    std::vector<int2> shifts_i;   // truncated to int, as the resample kernel receives them
+    std::vector<float2> tmpl;     // polar template [NR][256]
+    std::vector<float2> tw;       // e^(-2 pi i e / 256), e = 0..255
+    unsigned sbj_batch = 1;       // the reference's subject batch size
+};
+
+// Validates cfg exactly as every entry point does (recording the error on
+// failure) and fills the host tables.  Returns 0 or an error code.
+int host_geometry(const AlignConfig* cfg, HostGeometry& out);
+
+// Images of side dim per 2D linear texture on device dev.
+unsigned texture_images(int dev, unsigned dim);
+
+// Records an error for gpuisac_last_error and prints it.
+void record_error(int code, const char* msg);
+
+} // namespace gpuisac

@@ -42,7 +42,7 @@ EXPORTS = (
     "ref_free_alignment_2D_filter_references", "gpuisac_last_error", "gpuisac_clear_error",
     "gpuisac_version", "gpuisac_multi_ref_align_device", "gpuisac_spectra_device", "gpuisac_spectra_device_layout",
     "gpuisac_ccf_peak_device", "gpuisac_shift_count", "gpuisac_launch_count", "gpuisac_profile",
-    "gpuisac_kernel_time",
+    "gpuisac_kernel_time", "gpuisac_multi_ref_align_device_noalloc",
 )
 
 
@@ -85,6 +85,10 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_multi_ref_align_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.gpuisac_multi_ref_align_device.restype = ctypes.c_int
+    L.gpuisac_multi_ref_align_device_noalloc.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_void_p,
+                                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                         ctypes.c_void_p]
+    L.gpuisac_multi_ref_align_device_noalloc.restype = ctypes.c_int
     L.gpuisac_spectra_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.gpuisac_spectra_device.restype = ctypes.c_int

@@ -123,6 +123,22 @@ const char *gpuisac_version(void);
 int gpuisac_multi_ref_align_device(const AlignConfig *cfg, const float *sbj, const float *ref,
                                    const float *base_shift, float *d_out, float *peak_out, void *stream);
 
+/* No counterpart in the reference.  gpuisac_multi_ref_align_device without
+ * any device memory allocation, for callers that cannot call cudaMalloc:
+ * their GPU memory belongs to another allocator, or they must not pay the
+ * implicit synchronisation cudaMalloc / cudaFree can cause.  The work space is
+ * one 32 MiB array built into the library, held on every GPU that loads it
+ * until the process exits; a workload whose reference spectra plus one
+ * particle's spectra (ref_num + n_shift) * ring_num * 1 KiB exceed it is
+ * rejected with error 2.  The first call on a device looks up the array's
+ * device address (once per device); make that first call before any stream
+ * capture.  Every call shares the array, so calls that overlapped on the GPU
+ * would race: the entry point serialises its callers and returns only after
+ * its work on `stream` has finished.  Returns 0 or an error code. */
+int gpuisac_multi_ref_align_device_noalloc(const AlignConfig *cfg, const float *sbj, const float *ref,
+                                           const float *base_shift, float *d_out, float *peak_out,
+                                           void *stream);
+
 /* Ring spectra of a device image stack at every shift of cfg's grid, as the
  * CCF kernel consumes them: out [n_img][n_shift][ring_num][128][2] (float),
  * slot 0 = (F[0], F[128]); is_ref selects the reference layout (ring weight
