@@ -294,7 +294,7 @@ def bench_ours(args):
 
     # ---- end to end through the reference-facing C-ABI ----
     e2e = None
-    if rank == 0 or True:
+    if args.e2e_steps > 0:
         sp, rp = ptr_array(st.particles), ptr_array(st.refs)
         pl = np.zeros((R, 4 * P), np.float32)
         dh = np.zeros((R, P), np.float32)
