@@ -215,8 +215,10 @@ struct Workspace {
     std::vector<float2> geo_shifts;
     DevBuf<float2> tmpl, tw, shifts_f, ref_sp, sbj_sp, base;
     DevBuf<int2> shifts_i, zero_shift;
+    DevBuf<unsigned> err; // device-side timeout flag of the kernels' bounded waits
     void release()
     {
+        err.release();
         geo_D = geo_NR = 0;
         geo_shifts.clear();
         zero_shift.release();
@@ -261,6 +263,20 @@ int upload_geometry(const Geometry& g, Workspace& ws, cudaStream_t st)
     ws.geo_D = g.D;
     ws.geo_NR = g.NR;
     ws.geo_shifts = g.shifts_f;
+    return 0;
+}
+
+// after the stream has been synchronised: did a kernel give up a bounded wait?
+int check_device_flag(Workspace& ws)
+{
+    if (!ws.err.p)
+        return 0;
+    unsigned h = 0;
+    CK(cudaMemcpy(&h, ws.err.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (h) {
+        set_error(E_CUDA, "a kernel timed out waiting for its own asynchronous copies (flag %u)", h);
+        return E_CUDA;
+    }
     return 0;
 }
 
@@ -352,6 +368,9 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
     chunk = std::min<size_t>(chunk, g.P);
     if (ws.sbj_sp.ensure(per_part / sizeof(float2) * chunk))
         return E_NOMEM;
+    if (ws.err.ensure(1))
+        return E_NOMEM;
+    CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), st));
     for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk) {
         unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
         ev = g_timer.begin(st);
@@ -360,7 +379,7 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
         g_timer.end(K_SPECTRA, ev, st);
         ev = g_timer.begin(st);
         CK(launch_ccf_peak(ws.sbj_sp.p, ws.ref_sp.p, ws.tw.p, g.NR, g.S, g.R, n, p0, g.P, ws.shifts_f.p, d_base, d_out,
-                           d_peak, st));
+                           d_peak, ws.err.p, st));
         g_timer.end(K_CCF, ev, st);
     }
     return 0;
@@ -499,6 +518,9 @@ int do_multi_ref_align(State& s, const float** sbj_data, const float** ref_data,
     CK(cudaMemcpyAsync(peak_list, s.d_peak, (size_t)R * P * sizeof(float4), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
     g_timer.collect();
+    rc = check_device_flag(s.ws);
+    if (rc)
+        return rc;
     CK(cudaGetLastError());
     return 0;
 }
@@ -737,6 +759,9 @@ int gpuisac_multi_ref_align_device(const AlignConfig* cfg, const float* sbj, con
         return rc;
     CK(cudaStreamSynchronize(st));
     g_timer.collect();
+    rc = check_device_flag(ws);
+    if (rc)
+        return rc;
     CK(cudaGetLastError());
     return 0;
 }
@@ -803,9 +828,16 @@ int gpuisac_ccf_peak_device(const AlignConfig* cfg, const float* sbj_spectra, co
     rc = upload_geometry(g, ws, st);
     if (rc)
         return rc;
+    if (ws.err.ensure(1))
+        return E_NOMEM;
+    rc = check_device_flag(ws); // a previous asynchronous call's timeout, if any
+    CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), st));
+    if (rc)
+        return rc;
     CK(launch_ccf_peak(reinterpret_cast<const float2*>(sbj_spectra), reinterpret_cast<const float2*>(ref_spectra),
                        ws.tw.p, g.NR, g.S, g.R, n_part, p_global0, g.P, ws.shifts_f.p,
-                       reinterpret_cast<const float2*>(base_shift), d_out, reinterpret_cast<float4*>(peak_out), st));
+                       reinterpret_cast<const float2*>(base_shift), d_out, reinterpret_cast<float4*>(peak_out),
+                       ws.err.p, st));
     return 0;
 }
 

@@ -7,18 +7,30 @@
 // C2R of every ccf-table entry (:2453-2461), cu_aln_param_wizard (:1667-1794)
 // and the host scatter of multi_ref_align (:516-541).
 //
-// CTA = 256 threads, one tile of QT references (spectra resident in shared
-// memory), a run of particles.  Per iteration NSI = 16/QT shifts x QT refs =
-// 16 (shift, ref) pairs:
-//   contraction  thread (k = tid%128, half = tid/128) holds the subject
-//                spectra of NSI shifts at slot k and accumulates, for its
-//                QT/2 references, the four sums that form Z[k] and Z[256-k];
+// Both kernels run 256 threads and 16 (shift, reference) pairs per iteration:
+//   contraction  the four sums that form Z[k] and Z[256-k] (Z = O + iM, see
+//                polar_spectra.cu) for every slot k;
 //   inverse FFT  16 groups of 16 threads, one 256-point FFT per pair; real part
 //                = normal correlation, imaginary part = mirrored;
 //   peak search  first strict maximum in the reference's scan order
 //                (mirror-major, then shift, then angle), kept per pair slot
 //                with the 7 samples around it; merged per reference at the
 //                end of the particle, then the 7-point parabola.
+//
+// ccf_peak_tmem_kernel (up to 36 rings): 4 references per CTA held in tensor
+//   memory (lane = spectrum slot k, which is exactly the lane the thread
+//   owning slot k may read), split by ring halves across the two 128-thread
+//   halves (thread = slot k x half); the subject spectra of 4 shifts are
+//   staged into shared memory by bulk async copies (mbarrier, bounded wait)
+//   issued as soon as the previous contraction is done, so they overlap the
+//   FFT phase; the halves exchange partial sums through shared memory.
+// ccf_peak_kernel<QT> (any ring count up to the library maximum): QT
+//   references in shared memory, subject spectra loaded into registers in
+//   ring chunks.
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
 #include "gpuisac_device.cuh"
 #include "gpuisac_kernels.h"
 
@@ -56,8 +68,412 @@ __device__ float peak_angle(const float* x, unsigned tau, bool mirror)
     return angle;
 }
 
+// running best of one pair slot, replicated over its 16-thread group
+// (lanes 0..6 also hold the 7 samples around the peak)
+struct PeakState {
+    float bv;
+    unsigned bh, bt;
+    float nb;
+    __device__ void reset()
+    {
+        bv = -3.40282e+038f;
+        bh = 0;
+        bt = 0;
+        nb = 0.f;
+    }
+};
+
+// Z[k] and Z[256-k] of one pair from the four ring sums at slot k
+// (slot 0 carried (F[0], F[128]): recover the two real products)
+__device__ __forceinline__ void write_z(float2* zp, int k, float a1, float a2, float a3, float a4)
+{
+    if (k == 0) {
+        const float p1 = 0.25f * (a1 + a2 + a3 + a4);
+        const float p2 = 0.25f * (a1 - a2 + a3 - a4);
+        zp[0] = make_float2(p1, p1);
+        zp[kSlots] = make_float2(p2, p2);
+    } else {
+        zp[k] = make_float2(a1, a2);
+        zp[kRingLen - k] = make_float2(a3, a4);
+    }
+}
+
+// inverse FFT of the pair in gz and the peak search of both mirrors
+__device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, unsigned gmask, unsigned s,
+                                         unsigned n_shift, PeakState& st)
+{
+    float2 x[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++)
+        x[m] = gz[l + 16 * m];
+    fft256_group<+1>(x, gz, tw, l, gmask);
+    float* wf = reinterpret_cast<float*>(gz);
+#pragma unroll
+    for (int mir = 0; mir < 2; mir++) {
+        float v = mir ? x[perm16(0)].y : x[perm16(0)].x;
+        unsigned t = l;
+#pragma unroll
+        for (int k2 = 1; k2 < 16; k2++) {
+            const float c = mir ? x[perm16(k2)].y : x[perm16(k2)].x;
+            if (c > v) {
+                v = c;
+                t = l + 16 * k2;
+            }
+        }
+#pragma unroll
+        for (int off = 8; off > 0; off >>= 1) {
+            const float ov = __shfl_xor_sync(gmask, v, off);
+            const unsigned ot = __shfl_xor_sync(gmask, t, off);
+            if (ov > v || (ov == v && ot < t)) {
+                v = ov;
+                t = ot;
+            }
+        }
+        // lane 0's result for the whole group, so the branch below stays
+        // group-uniform even for NaN inputs
+        v = __shfl_sync(gmask, v, 0, 16);
+        t = __shfl_sync(gmask, t, 0, 16);
+        const unsigned hc = mir ? n_shift + s : s;
+        if (better(v, hc, t, st.bv, st.bh, st.bt)) {
+            st.bv = v;
+            st.bh = hc;
+            st.bt = t;
+            __syncwarp(gmask);
+#pragma unroll
+            for (int k2 = 0; k2 < 16; k2++)
+                wf[l + 16 * k2] = mir ? x[perm16(k2)].y : x[perm16(k2)].x;
+            __syncwarp(gmask);
+            if (l < 7)
+                st.nb = wf[(t + (unsigned)l - 3u) & (kRingLen - 1)];
+            __syncwarp(gmask);
+        }
+    }
+}
+
+// merge the nsi shift slots of each of the qt references and write the
+// outputs of particle p (all threads call; threads < qt write)
+__device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st, int tid, int g, int l, int qt,
+                                            int nsi, unsigned q0, unsigned n_ref, unsigned n_shift, unsigned pg,
+                                            unsigned p_total, const float2* shifts_f, const float2* base,
+                                            float* d_out, float4* peak_out)
+{
+    __syncthreads();
+    if (l == 0) {
+        slots[g].v = st.bv;
+        slots[g].h = st.bh;
+        slots[g].t = st.bt;
+    }
+    if (l < 7)
+        slots[g].nb[l] = st.nb;
+    __syncthreads();
+    if (tid < qt && q0 + tid < n_ref) {
+        int best = tid;
+        for (int i = 1; i < nsi; i++) {
+            const int c = i * qt + tid;
+            if (better(slots[c].v, slots[c].h, slots[c].t, slots[best].v, slots[best].h, slots[best].t))
+                best = c;
+        }
+        const PeakSlot& ps = slots[best];
+        const bool mirror = ps.h >= n_shift;
+        const unsigned sidx = mirror ? ps.h - n_shift : ps.h;
+        const float angle = peak_angle(ps.nb, ps.t, mirror);
+        const float bx = base ? base[pg].x : 0.f;
+        const float by = base ? base[pg].y : 0.f;
+        const float2 sf = shifts_f[sidx];
+        const size_t o = (size_t)(q0 + tid) * p_total + pg;
+        d_out[o] = ps.v;
+        peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+    }
+    __syncthreads();
+}
+
+// ---- mbarrier + bulk async copy (inline PTX) ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// bounded wait: gives up after ~2^22 polls (about a second with the back-off)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    for (uint32_t it = 0; it < (1u << 22); it++) {
+        if (mbar_test(bar, parity))
+            return true;
+        __nanosleep(it < 64 ? 0 : 256);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 } // namespace
 
+// ============================================================================
+// ---- tensor memory (inline PTX) ----
+namespace {
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst_smem)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// each thread of the warp writes 8 consecutive columns of its own lane
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+                 "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                 "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                 "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// 16 consecutive columns of the thread's own lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                 "%13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+} // namespace
+
+// ring-half kernel: references in tensor memory, subject spectra staged into
+// shared memory by bulk async copies (ring_num <= kTmaMaxRings)
+constexpr int kTmemRingsPerHalf = 18;
+constexpr uint32_t kTmemCols = 512;
+
+__global__ void __launch_bounds__(256, 1)
+ccf_peak_tmem_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ ref_sp,
+                     const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift, unsigned n_ref,
+                     unsigned n_part, unsigned part_per_cta, unsigned p_global0, unsigned p_total,
+                     const float2* __restrict__ shifts_f, const float2* __restrict__ base, float* __restrict__ d_out,
+                     float4* __restrict__ peak_out, unsigned* __restrict__ err)
+{
+    constexpr int QT = 4, NSI = 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned rh0 = (ring_num + 1) / 2; // rings of half 0 (half 1 has ring_num - rh0)
+    const unsigned nrp = 2 * rh0;            // rings per staged shift (one zero ring if odd)
+    float2* sbuf = reinterpret_cast<float2*>(smem_raw);                // [NSI][nrp][kSlots]
+    float2* zbuf = sbuf + (size_t)NSI * nrp * kSlots;                  // [16][kPairStride]
+    float* xbuf = reinterpret_cast<float*>(zbuf + 16 * kPairStride);   // [2][8][4][kSlots]
+    float2* tw = reinterpret_cast<float2*>(xbuf + 2 * 8 * 4 * kSlots); // [256]
+    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + kRingLen);      // [16]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(slots + 16);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int k = tid & (kSlots - 1);
+    const int half = tid >> 7;
+    const unsigned q0 = blockIdx.x * QT;
+    const unsigned p_begin = blockIdx.y * part_per_cta;
+    const unsigned p_end = min(n_part, p_begin + part_per_cta);
+    if (p_begin >= p_end)
+        return;
+
+    tw[tid] = twiddle[tid];
+    for (unsigned i = tid; i < (unsigned)NSI * nrp * kSlots; i += 256)
+        sbuf[i] = make_float2(0.f, 0.f); // the padding ring stays zero
+    if (warp == 0)
+        tmem_alloc(tmem_slot, kTmemCols);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    // lane k of the tensor memory holds slot k; columns: [half][ring][ref][u, v]
+    const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(half * kTmemRingsPerHalf * 8);
+    const unsigned r_base = half ? rh0 : 0u;
+    const unsigned rh = half ? ring_num - rh0 : rh0;
+    for (unsigned j = 0; j < (unsigned)kTmemRingsPerHalf; j++) {
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < QT; q++) {
+            float2 uv = make_float2(0.f, 0.f);
+            if (j < rh && q0 + q < n_ref)
+                uv = __ldg(&ref_sp[((size_t)(q0 + q) * ring_num + r_base + j) * kSlots + k]);
+            v[2 * q] = uv.x;
+            v[2 * q + 1] = uv.y;
+        }
+        tmem_st8(tmem + j * 8, v);
+    }
+    tmem_wait_st();
+
+    const uint32_t row_bytes = ring_num * kSlots * sizeof(float2);
+    // copies of shift group s0 of particle p (called by thread 0)
+    auto issue = [&](unsigned p, unsigned s0) {
+        unsigned nv = min((unsigned)NSI, n_shift - s0);
+        fence_proxy_async();
+        mbar_expect_tx(bar, nv * row_bytes);
+        for (unsigned i = 0; i < nv; i++)
+            bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sbj_sp + ((size_t)p * n_shift + s0 + i) * ring_num * kSlots,
+                     row_bytes, bar);
+    };
+    if (tid == 0)
+        issue(p_begin, 0);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    const int g = tid >> 4, l = tid & 15;
+    const unsigned gmask = 0xffffu << (tid & 16);
+    const int g_shift = g / QT;
+    float2* gz = zbuf + g * kPairStride;
+
+    for (unsigned p = p_begin; p < p_end && !failed; p++) {
+        PeakState st;
+        st.reset();
+        for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
+            // ---- wait for this group's spectra (bounded) ----
+            const bool ok = mbar_wait(bar, phase);
+            if (!__syncthreads_and(ok)) {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            // ---- contraction: this half's rings, 4 shifts x 4 references ----
+            float acc[QT][NSI][4];
+#pragma unroll
+            for (int q = 0; q < QT; q++)
+#pragma unroll
+                for (int i = 0; i < NSI; i++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        acc[q][i][c] = 0.f;
+            const float2* sb = sbuf + (size_t)r_base * kSlots + k;
+            for (unsigned j = 0; j < rh; j += 2) {
+                float rv[16]; // rings j, j+1: (u, v) of the 4 references
+                tmem_ld16(tmem + j * 8, rv);
+#pragma unroll
+                for (int jj = 0; jj < 2; jj++) {
+                    if (j + jj < rh) {
+                        float2 ab[NSI];
+#pragma unroll
+                        for (int i = 0; i < NSI; i++)
+                            ab[i] = sb[((size_t)i * nrp + j + jj) * kSlots];
+#pragma unroll
+                        for (int q = 0; q < QT; q++) {
+                            const float u = rv[jj * 8 + 2 * q], w = rv[jj * 8 + 2 * q + 1];
+#pragma unroll
+                            for (int i = 0; i < NSI; i++) {
+                                acc[q][i][0] = fmaf(u, ab[i].x, acc[q][i][0]);
+                                acc[q][i][1] = fmaf(u, ab[i].y, acc[q][i][1]);
+                                acc[q][i][2] = fmaf(w, ab[i].y, acc[q][i][2]);
+                                acc[q][i][3] = fmaf(w, ab[i].x, acc[q][i][3]);
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads(); // staging area read by everyone; previous FFT phase done with zbuf
+            // next group's copies overlap the exchange and the FFT phase
+            if (tid == 0) {
+                unsigned pn = p, sn = s0 + NSI;
+                if (sn >= n_shift) {
+                    pn = p + 1;
+                    sn = 0;
+                }
+                if (pn < p_end)
+                    issue(pn, sn);
+            }
+            // ---- exchange: half h owns shifts {2h, 2h+1} of the group ----
+#pragma unroll
+            for (int i = 0; i < NSI; i++) {
+                if ((i >> 1) != half) {
+#pragma unroll
+                    for (int q = 0; q < QT; q++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++)
+                            xbuf[(((half * 8) + (i & 1) * 4 + q) * 4 + c) * kSlots + k] = acc[q][i][c];
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int ii = 0; ii < 2; ii++) {
+                const int i = half * 2 + ii;
+#pragma unroll
+                for (int q = 0; q < QT; q++) {
+                    float s4[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        // compile-time indices on both sides keep acc in registers
+                        const float mine = half ? acc[q][2 + ii][c] : acc[q][ii][c];
+                        s4[c] = mine + xbuf[((((1 - half) * 8) + ii * 4 + q) * 4 + c) * kSlots + k];
+                    }
+                    write_z(zbuf + (i * QT + q) * kPairStride, k, s4[0], s4[1], s4[2], s4[3]);
+                }
+            }
+            __syncthreads();
+            // ---- inverse FFT + peak search, one pair per 16-thread group ----
+            const unsigned s = s0 + g_shift;
+            if (s < n_shift)
+                fft_peak(gz, tw, l, gmask, s, n_shift, st);
+        }
+        if (failed)
+            break;
+        merge_write(slots, st, tid, g, l, QT, NSI, q0, n_ref, n_shift, p_global0 + p, p_total, shifts_f, base, d_out,
+                    peak_out);
+    }
+    if (failed && tid == 0) {
+        atomicExch(err, 1u);
+        mbar_wait(bar, phase); // let copies in flight land before leaving
+    }
+    // release the tensor memory (all tcgen05 accesses of the CTA are done)
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 0)
+        tmem_dealloc(*tmem_slot, kTmemCols);
+}
+
+// ============================================================================
+// general kernel: references in shared memory, subject spectra in registers
 template <int QT>
 __global__ void __launch_bounds__(256, 1)
 ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ ref_sp,
@@ -106,9 +522,8 @@ ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ re
         const unsigned p = blockIdx.y * part_per_cta + pi;
         if (p >= n_part)
             break;
-        float bv = -3.40282e+038f;
-        unsigned bh = 0, bt = 0;
-        float nb = 0.f;
+        PeakState st;
+        st.reset();
 
         for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
             float acc[RPT][NSI][4];
@@ -128,25 +543,18 @@ ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ re
                 svalid[i] = s < n_shift;
                 srow[i] = sbj_sp + ((size_t)p * n_shift + (svalid[i] ? s : 0)) * ring_num * kSlots + k;
             }
-            float2 cur[NSI][RC], nxt[NSI][RC];
+            // ring chunks in two register buffers used alternately: the next
+            // chunk's loads are in flight while the current one is consumed
+            float2 bufa[NSI][RC], bufb[NSI][RC];
+            auto load = [&](float2 (&dst)[NSI][RC], unsigned r0) {
 #pragma unroll
-            for (int i = 0; i < NSI; i++)
+                for (int i = 0; i < NSI; i++)
 #pragma unroll
-                for (int rr = 0; rr < RC; rr++)
-                    cur[i][rr] = (svalid[i] && (unsigned)rr < ring_num) ? __ldg(srow[i] + rr * kSlots)
-                                                                        : make_float2(0.f, 0.f);
-            for (unsigned c = 0; c < n_chunks; c++) {
-                const unsigned r0 = c * RC;
-                if (c + 1 < n_chunks) {
-                    const unsigned r1 = r0 + RC;
-#pragma unroll
-                    for (int i = 0; i < NSI; i++)
-#pragma unroll
-                        for (int rr = 0; rr < RC; rr++)
-                            nxt[i][rr] = (svalid[i] && r1 + rr < ring_num)
-                                             ? __ldg(srow[i] + (size_t)(r1 + rr) * kSlots)
-                                             : make_float2(0.f, 0.f);
-                }
+                    for (int rr = 0; rr < RC; rr++)
+                        dst[i][rr] = (svalid[i] && r0 + rr < ring_num) ? __ldg(srow[i] + (size_t)(r0 + rr) * kSlots)
+                                                                       : make_float2(0.f, 0.f);
+            };
+            auto consume = [&](const float2 (&src)[NSI][RC], unsigned r0) {
 #pragma unroll
                 for (int j = 0; j < RPT; j++) {
                     const float2* rq = rsp + ((size_t)(half * RPT + j) * nrp + r0) * kSlots + k;
@@ -155,7 +563,7 @@ ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ re
                         const float2 uv = rq[rr * kSlots];
 #pragma unroll
                         for (int i = 0; i < NSI; i++) {
-                            const float2 ab = cur[i][rr];
+                            const float2 ab = src[i][rr];
                             acc[j][i][0] = fmaf(uv.x, ab.x, acc[j][i][0]);
                             acc[j][i][1] = fmaf(uv.x, ab.y, acc[j][i][1]);
                             acc[j][i][2] = fmaf(uv.y, ab.y, acc[j][i][2]);
@@ -163,125 +571,63 @@ ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ re
                         }
                     }
                 }
-#pragma unroll
-                for (int i = 0; i < NSI; i++)
-#pragma unroll
-                    for (int rr = 0; rr < RC; rr++)
-                        cur[i][rr] = nxt[i][rr];
+            };
+            load(bufa, 0);
+            for (unsigned c = 0; c < n_chunks; c += 2) {
+                if (c + 1 < n_chunks)
+                    load(bufb, (c + 1) * RC);
+                consume(bufa, c * RC);
+                if (c + 1 < n_chunks) {
+                    if (c + 2 < n_chunks)
+                        load(bufa, (c + 2) * RC);
+                    consume(bufb, (c + 1) * RC);
+                }
             }
 
             __syncthreads(); // previous FFT phase is done with zbuf
 #pragma unroll
-            for (int j = 0; j < RPT; j++) {
+            for (int j = 0; j < RPT; j++)
 #pragma unroll
-                for (int i = 0; i < NSI; i++) {
-                    float2* zp = zbuf + (i * QT + half * RPT + j) * kPairStride;
-                    const float a1 = acc[j][i][0], a2 = acc[j][i][1], a3 = acc[j][i][2], a4 = acc[j][i][3];
-                    if (k == 0) {
-                        // slot 0 carried (F[0], F[128]): recover the two real products
-                        const float p1 = 0.25f * (a1 + a2 + a3 + a4);
-                        const float p2 = 0.25f * (a1 - a2 + a3 - a4);
-                        zp[0] = make_float2(p1, p1);
-                        zp[kSlots] = make_float2(p2, p2);
-                    } else {
-                        zp[k] = make_float2(a1, a2);
-                        zp[kRingLen - k] = make_float2(a3, a4);
-                    }
-                }
-            }
+                for (int i = 0; i < NSI; i++)
+                    write_z(zbuf + (i * QT + half * RPT + j) * kPairStride, k, acc[j][i][0], acc[j][i][1],
+                            acc[j][i][2], acc[j][i][3]);
             __syncthreads();
 
-            // ---- inverse FFT + peak search, one pair per 16-thread group ----
             const unsigned s = s0 + g_shift;
-            if (s < n_shift) {
-                float2 x[16];
-#pragma unroll
-                for (int m = 0; m < 16; m++)
-                    x[m] = gz[l + 16 * m];
-                fft256_group<+1>(x, gz, tw, l, gmask);
-                float* wf = reinterpret_cast<float*>(gz);
-#pragma unroll
-                for (int mir = 0; mir < 2; mir++) {
-                    float v = mir ? x[0].y : x[0].x;
-                    unsigned t = l;
-#pragma unroll
-                    for (int k2 = 1; k2 < 16; k2++) {
-                        const float c = mir ? x[k2].y : x[k2].x;
-                        if (c > v) {
-                            v = c;
-                            t = l + 16 * k2;
-                        }
-                    }
-#pragma unroll
-                    for (int off = 8; off > 0; off >>= 1) {
-                        const float ov = __shfl_xor_sync(gmask, v, off);
-                        const unsigned ot = __shfl_xor_sync(gmask, t, off);
-                        if (ov > v || (ov == v && ot < t)) {
-                            v = ov;
-                            t = ot;
-                        }
-                    }
-                    // lane 0's result for the whole group, so the branch below
-                    // stays group-uniform even for NaN inputs
-                    v = __shfl_sync(gmask, v, 0, 16);
-                    t = __shfl_sync(gmask, t, 0, 16);
-                    const unsigned hc = mir ? n_shift + s : s;
-                    if (better(v, hc, t, bv, bh, bt)) {
-                        bv = v;
-                        bh = hc;
-                        bt = t;
-                        __syncwarp(gmask);
-#pragma unroll
-                        for (int k2 = 0; k2 < 16; k2++)
-                            wf[l + 16 * k2] = mir ? x[k2].y : x[k2].x;
-                        __syncwarp(gmask);
-                        if (l < 7)
-                            nb = wf[(t + (unsigned)l - 3u) & (kRingLen - 1)];
-                        __syncwarp(gmask);
-                    }
-                }
-            }
+            if (s < n_shift)
+                fft_peak(gz, tw, l, gmask, s, n_shift, st);
         }
-
-        // ---- merge the NSI shift slots of each reference, write results ----
-        __syncthreads();
-        if (l == 0) {
-            slots[g].v = bv;
-            slots[g].h = bh;
-            slots[g].t = bt;
-        }
-        if (l < 7)
-            slots[g].nb[l] = nb;
-        __syncthreads();
-        if (tid < QT && q0 + tid < n_ref) {
-            int best = tid;
-#pragma unroll
-            for (int i = 1; i < NSI; i++) {
-                const int c = i * QT + tid;
-                if (better(slots[c].v, slots[c].h, slots[c].t, slots[best].v, slots[best].h, slots[best].t))
-                    best = c;
-            }
-            const PeakSlot& ps = slots[best];
-            const bool mirror = ps.h >= n_shift;
-            const unsigned sidx = mirror ? ps.h - n_shift : ps.h;
-            const float angle = peak_angle(ps.nb, ps.t, mirror);
-            const unsigned pg = p_global0 + p;
-            const float bx = base ? base[pg].x : 0.f;
-            const float by = base ? base[pg].y : 0.f;
-            const float2 sf = shifts_f[sidx];
-            const size_t o = (size_t)(q0 + tid) * p_total + pg;
-            d_out[o] = ps.v;
-            peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
-        }
-        __syncthreads();
+        merge_write(slots, st, tid, g, l, QT, NSI, q0, n_ref, n_shift, p_global0 + p, p_total, shifts_f, base, d_out,
+                    peak_out);
     }
+}
+
+// ============================================================================
+constexpr unsigned kTmaMaxRings = 2 * kTmemRingsPerHalf;
+
+static size_t tma_smem_bytes(unsigned ring_num)
+{
+    unsigned nrp = 2 * ((ring_num + 1) / 2);
+    return (size_t)4 * nrp * kSlots * sizeof(float2) + 16 * kPairStride * sizeof(float2) +
+           2 * 8 * 4 * kSlots * sizeof(float) + kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16;
 }
 
 size_t ccf_peak_smem_bytes(unsigned ring_num)
 {
+    if (ring_num <= kTmaMaxRings)
+        return tma_smem_bytes(ring_num);
     unsigned qt = ccf_refs_per_cta(ring_num);
     return (size_t)qt * ring_pad(ring_num) * kSlots * sizeof(float2) + 16 * kPairStride * sizeof(float2) +
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot);
+}
+
+template <typename K>
+static cudaError_t set_max_smem(K kernel)
+{
+    int dev = 0, max_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin);
 }
 
 template <int QT>
@@ -291,13 +637,8 @@ static cudaError_t launch_qt(const float2* sbj_sp, const float2* ref_sp, const f
                              float4* peak_out, cudaStream_t stream)
 {
     static int configured = 0;
-    size_t smem = ccf_peak_smem_bytes(ring_num);
     if (!configured) {
-        int dev = 0, max_optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cudaError_t e = cudaFuncSetAttribute(ccf_peak_kernel<QT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             max_optin);
+        cudaError_t e = set_max_smem(ccf_peak_kernel<QT>);
         if (e != cudaSuccess)
             return e;
         configured = 1;
@@ -305,8 +646,31 @@ static cudaError_t launch_qt(const float2* sbj_sp, const float2* ref_sp, const f
     const unsigned ref_tiles = (n_ref + QT - 1) / QT;
     const unsigned ppc = 8;
     dim3 grid(ref_tiles, (n_part + ppc - 1) / ppc);
-    ccf_peak_kernel<QT><<<grid, 256, smem, stream>>>(sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, ppc,
-                                                     p_global0, p_total, shifts_f, base, d_out, peak_out);
+    ccf_peak_kernel<QT><<<grid, 256, ccf_peak_smem_bytes(ring_num), stream>>>(
+        sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, ppc, p_global0, p_total, shifts_f, base, d_out,
+        peak_out);
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_tmem(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle, unsigned ring_num,
+                               unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_global0,
+                               unsigned p_total, const float2* shifts_f, const float2* base, float* d_out,
+                               float4* peak_out, unsigned* err, cudaStream_t stream)
+{
+    static int configured = 0;
+    if (!configured) {
+        cudaError_t e = set_max_smem(ccf_peak_tmem_kernel);
+        if (e != cudaSuccess)
+            return e;
+        configured = 1;
+    }
+    const unsigned ref_tiles = (n_ref + 3) / 4;
+    const unsigned ppc = 8;
+    dim3 grid(ref_tiles, (n_part + ppc - 1) / ppc);
+    ccf_peak_tmem_kernel<<<grid, 256, tma_smem_bytes(ring_num), stream>>>(
+        sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, ppc, p_global0, p_total, shifts_f, base, d_out,
+        peak_out, err);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }
@@ -314,10 +678,18 @@ static cudaError_t launch_qt(const float2* sbj_sp, const float2* ref_sp, const f
 cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle, unsigned ring_num,
                             unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_global0, unsigned p_total,
                             const float2* shifts_f, const float2* base, float* d_out, float4* peak_out,
-                            cudaStream_t stream)
+                            unsigned* err, cudaStream_t stream)
 {
     if (n_part == 0 || n_ref == 0)
         return cudaSuccess;
+    // GPUISAC_CCF_KERNEL=general selects the general kernel for every ring count
+    const char* sel = getenv("GPUISAC_CCF_KERNEL");
+    const bool force_general = sel && strcmp(sel, "general") == 0;
+    // bulk copies need 16-byte aligned sources (every row is a multiple of 1 KiB)
+    const bool aligned = ((uintptr_t)sbj_sp & 15) == 0;
+    if (ring_num <= kTmaMaxRings && err && aligned && !force_general)
+        return launch_tmem(sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, p_global0, p_total, shifts_f,
+                           base, d_out, peak_out, err, stream);
     if (ccf_refs_per_cta(ring_num) == 4)
         return launch_qt<4>(sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, p_global0, p_total, shifts_f,
                             base, d_out, peak_out, stream);

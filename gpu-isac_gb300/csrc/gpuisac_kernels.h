@@ -42,9 +42,12 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
 // whose spectra are in sbj_sp ([n_part][n_shift][ring_num][kSlots]); results
 // for particle i go to column p_global0 + i of d_out [n_ref][p_total] and
 // peak_out [n_ref][p_total] (angle, shift_x, shift_y, mirror).
+// err: device word set to non-zero if a kernel gave up waiting for its own
+// asynchronous copies (bounded waits; the host checks it after the stream).
 cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle,
                             unsigned ring_num, unsigned n_shift, unsigned n_ref, unsigned n_part,
                             unsigned p_global0, unsigned p_total, const float2* shifts_f,
-                            const float2* base, float* d_out, float4* peak_out, cudaStream_t stream);
+                            const float2* base, float* d_out, float4* peak_out, unsigned* err,
+                            cudaStream_t stream);
 
 } // namespace gpuisac

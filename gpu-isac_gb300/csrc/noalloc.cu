@@ -73,7 +73,8 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
     // carve the array: tables, reference spectra, then as many particles'
     // spectra as fit
     const size_t row_bytes = (size_t)g.NR * kSlots * sizeof(float2); // one (image, shift) row
-    const size_t off_tw = 0;
+    const size_t off_err = 0;
+    const size_t off_tw = off_err + 256;
     const size_t off_zero = off_tw + up256(kRingLen * sizeof(float2));
     const size_t off_tmpl = off_zero + up256(sizeof(int2));
     const size_t off_sf = off_tmpl + up256(g.tmpl.size() * sizeof(float2));
@@ -105,6 +106,7 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
         g_noalloc_dev[dev] = static_cast<unsigned char*>(p);
     }
     unsigned char* base = g_noalloc_dev[dev];
+    unsigned* err = reinterpret_cast<unsigned*>(base + off_err);
     float2* tw = reinterpret_cast<float2*>(base + off_tw);
     int2* zero = reinterpret_cast<int2*>(base + off_zero);
     float2* tmpl = reinterpret_cast<float2*>(base + off_tmpl);
@@ -115,6 +117,7 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int2 zero_h = make_int2(0, 0);
+    NA_CK(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
     NA_CK(cudaMemcpyAsync(tw, g.tw.data(), kRingLen * sizeof(float2), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(zero, &zero_h, sizeof(int2), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(tmpl, g.tmpl.data(), g.tmpl.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
@@ -133,9 +136,13 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
         const unsigned n = std::min(chunk, g.P - p0);
         NA_CK(launch_polar_spectra(sbjs, tmpl, tw, g.NR, si, g.S, bs, p0, n, 0, sbj_sp, st));
         NA_CK(launch_ccf_peak(sbj_sp, ref_sp, tw, g.NR, g.S, g.R, n, p0, g.P, sf, bs, d_out,
-                              reinterpret_cast<float4*>(peak_out), st));
+                              reinterpret_cast<float4*>(peak_out), err, st));
     }
     // the host tables and the shared array must outlive the work
     NA_CK(cudaStreamSynchronize(st));
+    unsigned flag = 0;
+    NA_CK(cudaMemcpy(&flag, err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (flag)
+        return fail(1, "a kernel timed out waiting for its own asynchronous copies");
     return 0;
 }

@@ -113,7 +113,7 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
         // natural-order spectrum Z[l + 16 k2] to the workspace
 #pragma unroll
         for (int k2 = 0; k2 < 16; k2++)
-            gws[l + 16 * k2] = x[k2];
+            gws[l + 16 * k2] = x[perm16(k2)];
         __syncwarp(gmask);
         // unpack the two real spectra and write slots k = l + 16 i (i = 0..7)
 #pragma unroll

@@ -64,6 +64,24 @@ void orc_tex_split(float t, int *i, float *a)
     *a = (float)((q - fi * 256.0) / 256.0);
 }
 
+/* Texture unit bilinear weights of one sample point, in units of 1/256:
+ * the two 8-bit fractions A (x) and B (y) give w11 = round(A*B/256) (ties
+ * upward) and the other three taps take what is left of each fraction, so
+ * the four weights always sum to 256.  Pinned against the hardware by
+ * tests/test_gpu_texture.py. */
+void orc_tex_weights(float x, float y, int *ix, int *iy, int w[4])
+{
+    float ax, ay;
+    orc_tex_split(x, ix, &ax);
+    orc_tex_split(y, iy, &ay);
+    int A = (int)(ax * 256.0f), B = (int)(ay * 256.0f);
+    int w11 = (A * B + 128) >> 8;
+    w[0] = 256 - A - B + w11; /* (ix,   iy)   */
+    w[1] = A - w11;           /* (ix+1, iy)   */
+    w[2] = B - w11;           /* (ix,   iy+1) */
+    w[3] = w11;               /* (ix+1, iy+1) */
+}
+
 /* Reference: multi_ref_align batch sizing, cuda/gpu_aln_noref.cu:429-440 with
  * the cuFFT int32 guard of multi_ref_align_size_check (:238). */
 unsigned orc_reference_sbj_batch(const orc_cfg *cfg)

@@ -74,6 +74,10 @@ int orc_shift_array(float rng_x, float rng_y, float step, float *out_xy, int cap
  * (after the 8-bit rounding) and the weight a in [0,1) in 1/256 steps. */
 void orc_tex_split(float t, int *i, float *a);
 
+/* Bilinear tap weights (units of 1/256, summing to 256) of the texture unit
+ * at texel-space point (x, y): w = {(ix,iy), (ix+1,iy), (ix,iy+1), (ix+1,iy+1)}. */
+void orc_tex_weights(float x, float y, int *ix, int *iy, int w[4]);
+
 /* Reference subject batch size for this config (the cuFFT int32 guard of
  * noref.cu:238; the device-memory half of that check is assumed to pass). */
 unsigned orc_reference_sbj_batch(const orc_cfg *cfg);

@@ -114,15 +114,12 @@ static int FN(polar_ctx)(const FN(ctx) *c, const orc_cfg *cfg, const orc_layout 
             float oy = c->tmpl[(r * L + j) * 2 + 1];
             float x = cnt_x + ox;
             float y = (yoff + cnt_y) + oy;
-            int ix, iy;
-            float ax, ay;
-            orc_tex_split(x, &ix, &ax);
-            orc_tex_split(y, &iy, &ay);
+            int ix, iy, w[4];
+            orc_tex_weights(x, y, &ix, &iy, w);
             REAL t00 = texel(&ts, img, iy, ix), t10 = texel(&ts, img, iy, ix + 1);
             REAL t01 = texel(&ts, img, iy + 1, ix), t11 = texel(&ts, img, iy + 1, ix + 1);
-            REAL a = (REAL)ax, b = (REAL)ay;
-            out[(size_t)r * L + j] = (1 - a) * (1 - b) * t00 + a * (1 - b) * t10 +
-                                     (1 - a) * b * t01 + a * b * t11;
+            out[(size_t)r * L + j] = ((REAL)w[0] * t00 + (REAL)w[1] * t10 + (REAL)w[2] * t01 +
+                                      (REAL)w[3] * t11) * (REAL)(1.0 / 256.0);
         }
     }
 

@@ -56,6 +56,8 @@ def lib():
         L.orc_shift_array.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, fp, ctypes.c_int]
         L.orc_shift_array.restype = ctypes.c_int
         L.orc_tex_split.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_int), fp]
+        L.orc_tex_weights.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.orc_reference_sbj_batch.argtypes = [cfgp]
         L.orc_reference_sbj_batch.restype = ctypes.c_uint
         for pfx, rp in (("f64", dp), ("f32", fp)):
@@ -115,6 +117,14 @@ def tex_split(t: float):
     a = ctypes.c_float()
     lib().orc_tex_split(t, ctypes.byref(i), ctypes.byref(a))
     return i.value, a.value
+
+
+def tex_weights(x: float, y: float):
+    """(ix, iy, [w00, w10, w01, w11]) in units of 1/256"""
+    ix, iy = ctypes.c_int(), ctypes.c_int()
+    w = (ctypes.c_int * 4)()
+    lib().orc_tex_weights(x, y, ctypes.byref(ix), ctypes.byref(iy), w)
+    return ix.value, iy.value, list(w)
 
 
 def _real(precision):

@@ -42,12 +42,11 @@ def emulate(oracle_mod, img, xy):
     H, W = img.shape
     out = np.zeros(len(xy))
     for n, (x, y) in enumerate(xy):
-        ix, ax = oracle_mod.tex_split(float(x))
-        iy, ay = oracle_mod.tex_split(float(y))
+        ix, iy, w = oracle_mod.tex_weights(float(x), float(y))
         x0, x1 = np.clip([ix, ix + 1], 0, W - 1)
         y0, y1 = np.clip([iy, iy + 1], 0, H - 1)
-        out[n] = ((1 - ax) * (1 - ay) * img[y0, x0] + ax * (1 - ay) * img[y0, x1] +
-                  (1 - ax) * ay * img[y1, x0] + ax * ay * img[y1, x1])
+        out[n] = (w[0] * float(img[y0, x0]) + w[1] * float(img[y0, x1]) + w[2] * float(img[y1, x0]) +
+                  w[3] * float(img[y1, x1])) / 256.0
     return out
 
 
@@ -59,6 +58,17 @@ def test_weight_quantisation_and_rounding(probe, oracle_mod):
     hw = probe(img, xy)
     em = emulate(oracle_mod, img, xy)
     assert np.array_equal(hw, em.astype(np.float32)), np.c_[fr, hw, em][hw != em][:10]
+
+
+def test_tap_weights_single_texel(probe, oracle_mod):
+    """One texel of 256 on a zero image: each filtered value is one tap weight."""
+    rng = np.random.default_rng(7)
+    img = np.zeros((16, 16), np.float32)
+    img[7, 7] = 256.0
+    xy = np.stack([rng.uniform(6.5, 8.5, 6000), rng.uniform(6.5, 8.5, 6000)], 1).astype(np.float32)
+    hw = probe(img, xy)
+    em = emulate(oracle_mod, img, xy)
+    assert np.array_equal(hw, em.astype(np.float32))
 
 
 def test_random_coordinates_match(probe, oracle_mod):

@@ -46,6 +46,15 @@ def test_texture_weight_rounding(oracle_mod, t, expect):
     assert (i, a) == expect
 
 
+@pytest.mark.parametrize("fx,fy", [(0.0, 0.0), (221.0, 128.0), (196.0, 32.0), (128.0, 128.0), (255.0, 255.0)])
+def test_texture_tap_weights(oracle_mod, fx, fy):
+    ix, iy, w = oracle_mod.tex_weights(10.5 + fx / 256.0, 20.5 + fy / 256.0)
+    A, B = int(fx), int(fy)
+    w11 = (A * B + 128) >> 8
+    assert (ix, iy) == (10, 20) and sum(w) == 256
+    assert w == [256 - A - B + w11, A - w11, B - w11, w11]
+
+
 def test_reference_layout_config1(oracle_mod):
     cfg = oracle_mod.make_cfg(50000, 200, 76, 35, 256, 1.0, 3.0, 3.0)
     lay = oracle_mod.reference_layout(cfg)
