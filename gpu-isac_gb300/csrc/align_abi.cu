@@ -565,6 +565,8 @@ int host_geometry(const AlignConfig* cfg, HostGeometry& out)
     return 0;
 }
 
+unsigned reference_batch(const AlignConfig* cfg) { return std::max(1u, reference_sbj_batch(cfg)); }
+
 unsigned texture_images(int dev, unsigned dim) { return std::max(1u, texture_image_limit(dev, std::max(dim, 1u))); }
 
 void record_error(int code, const char* msg) { set_error(code, "%s", msg); }

@@ -31,6 +31,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+
 #include "gpuisac_device.cuh"
 #include "gpuisac_kernels.h"
 
@@ -110,31 +112,31 @@ __device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, un
     float* wf = reinterpret_cast<float*>(gz);
 #pragma unroll
     for (int mir = 0; mir < 2; mir++) {
+        // group maximum first; the first index is only needed when this
+        // candidate can replace the running best
         float v = mir ? x[perm16(0)].y : x[perm16(0)].x;
-        unsigned t = l;
 #pragma unroll
-        for (int k2 = 1; k2 < 16; k2++) {
-            const float c = mir ? x[perm16(k2)].y : x[perm16(k2)].x;
-            if (c > v) {
-                v = c;
-                t = l + 16 * k2;
-            }
-        }
+        for (int k2 = 1; k2 < 16; k2++)
+            v = fmaxf(v, mir ? x[perm16(k2)].y : x[perm16(k2)].x);
 #pragma unroll
-        for (int off = 8; off > 0; off >>= 1) {
-            const float ov = __shfl_xor_sync(gmask, v, off);
-            const unsigned ot = __shfl_xor_sync(gmask, t, off);
-            if (ov > v || (ov == v && ot < t)) {
-                v = ov;
-                t = ot;
-            }
-        }
-        // lane 0's result for the whole group, so the branch below stays
-        // group-uniform even for NaN inputs
+        for (int off = 8; off > 0; off >>= 1)
+            v = fmaxf(v, __shfl_xor_sync(gmask, v, off));
+        // lane 0's value for the whole group keeps every branch below
+        // group-uniform, NaN inputs included
         v = __shfl_sync(gmask, v, 0, 16);
+        if (!(v >= st.bv))
+            continue;
+        unsigned t = 0xffffffffu;
+#pragma unroll
+        for (int k2 = 15; k2 >= 0; k2--)
+            if ((mir ? x[perm16(k2)].y : x[perm16(k2)].x) == v)
+                t = l + 16 * k2;
+#pragma unroll
+        for (int off = 8; off > 0; off >>= 1)
+            t = min(t, __shfl_xor_sync(gmask, t, off));
         t = __shfl_sync(gmask, t, 0, 16);
         const unsigned hc = mir ? n_shift + s : s;
-        if (better(v, hc, t, st.bv, st.bh, st.bt)) {
+        if (t < (unsigned)kRingLen && better(v, hc, t, st.bv, st.bh, st.bt)) {
             st.bv = v;
             st.bh = hc;
             st.bt = t;
@@ -282,17 +284,45 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 }
 } // namespace
 
+// ---- work items ----
+// Work item = (group, reference tile, block of up to ppc particles).  Items of
+// a group are numbered reference tile fastest, so consecutive items (running
+// on different SMs at the same time) read the same particles' spectra.
+__device__ __forceinline__ bool decode_item(const CcfWork& w, unsigned item, int qt, CcfGroup& grp, unsigned& q0,
+                                            unsigned& pb, unsigned& pe)
+{
+    if (item >= w.n_items)
+        return false;
+    if (w.groups == nullptr) {
+        grp = w.one;
+    } else {
+        unsigned lo = 0, hi = w.n_groups - 1; // last group with item_begin <= item
+        while (lo < hi) {
+            const unsigned mid = (lo + hi + 1) >> 1;
+            if (w.groups[mid].item_begin <= item)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        grp = w.groups[lo];
+    }
+    const unsigned local = item - grp.item_begin;
+    const unsigned tile = local % grp.ref_tiles, blk = local / grp.ref_tiles;
+    q0 = tile * (unsigned)qt;
+    pb = blk * w.ppc;
+    pe = min(grp.n_part, pb + w.ppc);
+    return pb < pe;
+}
+
 // ring-half kernel: references in tensor memory, subject spectra staged into
-// shared memory by bulk async copies (ring_num <= kTmaMaxRings)
+// shared memory by bulk async copies (ring_num <= kTmaMaxRings); persistent
+// over work items
 constexpr int kTmemRingsPerHalf = 18;
 constexpr uint32_t kTmemCols = 512;
 
 __global__ void __launch_bounds__(256, 1)
-ccf_peak_tmem_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ ref_sp,
-                     const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift, unsigned n_ref,
-                     unsigned n_part, unsigned part_per_cta, unsigned p_global0, unsigned p_total,
-                     const float2* __restrict__ shifts_f, const float2* __restrict__ base, float* __restrict__ d_out,
-                     float4* __restrict__ peak_out, unsigned* __restrict__ err)
+ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift,
+                     const float2* __restrict__ shifts_f, unsigned* __restrict__ err)
 {
     constexpr int QT = 4, NSI = 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -310,10 +340,11 @@ ccf_peak_tmem_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict
     const int warp = tid >> 5;
     const int k = tid & (kSlots - 1);
     const int half = tid >> 7;
-    const unsigned q0 = blockIdx.x * QT;
-    const unsigned p_begin = blockIdx.y * part_per_cta;
-    const unsigned p_end = min(n_part, p_begin + part_per_cta);
-    if (p_begin >= p_end)
+
+    unsigned item = blockIdx.x;
+    CcfGroup grp;
+    unsigned q0, pb, pe;
+    if (!decode_item(w, item, QT, grp, q0, pb, pe))
         return;
 
     tw[tid] = twiddle[tid];
@@ -332,32 +363,19 @@ ccf_peak_tmem_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict
     const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(half * kTmemRingsPerHalf * 8);
     const unsigned r_base = half ? rh0 : 0u;
     const unsigned rh = half ? ring_num - rh0 : rh0;
-    for (unsigned j = 0; j < (unsigned)kTmemRingsPerHalf; j++) {
-        float v[8];
-#pragma unroll
-        for (int q = 0; q < QT; q++) {
-            float2 uv = make_float2(0.f, 0.f);
-            if (j < rh && q0 + q < n_ref)
-                uv = __ldg(&ref_sp[((size_t)(q0 + q) * ring_num + r_base + j) * kSlots + k]);
-            v[2 * q] = uv.x;
-            v[2 * q + 1] = uv.y;
-        }
-        tmem_st8(tmem + j * 8, v);
-    }
-    tmem_wait_st();
-
     const uint32_t row_bytes = ring_num * kSlots * sizeof(float2);
-    // copies of shift group s0 of particle p (called by thread 0)
-    auto issue = [&](unsigned p, unsigned s0) {
+
+    // copies of shift group s0 of particle p of group g (called by thread 0)
+    auto issue = [&](const float2* sp, unsigned p, unsigned s0) {
         unsigned nv = min((unsigned)NSI, n_shift - s0);
         fence_proxy_async();
         mbar_expect_tx(bar, nv * row_bytes);
         for (unsigned i = 0; i < nv; i++)
-            bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sbj_sp + ((size_t)p * n_shift + s0 + i) * ring_num * kSlots,
+            bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sp + ((size_t)p * n_shift + s0 + i) * ring_num * kSlots,
                      row_bytes, bar);
     };
     if (tid == 0)
-        issue(p_begin, 0);
+        issue(grp.sbj_sp, pb, 0);
     uint32_t phase = 0;
     bool failed = false;
 
@@ -366,99 +384,130 @@ ccf_peak_tmem_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict
     const int g_shift = g / QT;
     float2* gz = zbuf + g * kPairStride;
 
-    for (unsigned p = p_begin; p < p_end && !failed; p++) {
-        PeakState st;
-        st.reset();
-        for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
-            // ---- wait for this group's spectra (bounded) ----
-            const bool ok = mbar_wait(bar, phase);
-            if (!__syncthreads_and(ok)) {
-                failed = true;
-                break;
+    while (!failed) {
+        // this item's references -> tensor memory (each thread writes the
+        // columns it will read itself)
+        for (unsigned j = 0; j < (unsigned)kTmemRingsPerHalf; j++) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < QT; q++) {
+                float2 uv = make_float2(0.f, 0.f);
+                if (j < rh && q0 + q < grp.n_ref)
+                    uv = __ldg(&grp.ref_sp[((size_t)(q0 + q) * ring_num + r_base + j) * kSlots + k]);
+                v[2 * q] = uv.x;
+                v[2 * q + 1] = uv.y;
             }
-            phase ^= 1u;
-            // ---- contraction: this half's rings, 4 shifts x 4 references ----
-            float acc[QT][NSI][4];
+            tmem_st8(tmem + j * 8, v);
+        }
+        tmem_wait_st();
+        // the item after this one, for the copies issued at its end
+        CcfGroup ngrp;
+        unsigned nq0 = 0, npb = 0, npe = 0;
+        const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
+
+        for (unsigned p = pb; p < pe && !failed; p++) {
+            PeakState st;
+            st.reset();
+            for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
+                // ---- wait for this group's spectra (bounded) ----
+                const bool ok = mbar_wait(bar, phase);
+                if (!__syncthreads_and(ok)) {
+                    failed = true;
+                    break;
+                }
+                phase ^= 1u;
+                // ---- contraction: this half's rings, 4 shifts x 4 references ----
+                float acc[QT][NSI][4];
 #pragma unroll
-            for (int q = 0; q < QT; q++)
+                for (int q = 0; q < QT; q++)
 #pragma unroll
-                for (int i = 0; i < NSI; i++)
+                    for (int i = 0; i < NSI; i++)
 #pragma unroll
-                    for (int c = 0; c < 4; c++)
-                        acc[q][i][c] = 0.f;
-            const float2* sb = sbuf + (size_t)r_base * kSlots + k;
-            for (unsigned j = 0; j < rh; j += 2) {
-                float rv[16]; // rings j, j+1: (u, v) of the 4 references
-                tmem_ld16(tmem + j * 8, rv);
+                        for (int c = 0; c < 4; c++)
+                            acc[q][i][c] = 0.f;
+                const float2* sb = sbuf + (size_t)r_base * kSlots + k;
+                for (unsigned j = 0; j < rh; j += 2) {
+                    float rv[16]; // rings j, j+1: (u, v) of the 4 references
+                    tmem_ld16(tmem + j * 8, rv);
 #pragma unroll
-                for (int jj = 0; jj < 2; jj++) {
-                    if (j + jj < rh) {
-                        float2 ab[NSI];
+                    for (int jj = 0; jj < 2; jj++) {
+                        if (j + jj < rh) {
+                            float2 ab[NSI];
 #pragma unroll
-                        for (int i = 0; i < NSI; i++)
-                            ab[i] = sb[((size_t)i * nrp + j + jj) * kSlots];
+                            for (int i = 0; i < NSI; i++)
+                                ab[i] = sb[((size_t)i * nrp + j + jj) * kSlots];
 #pragma unroll
-                        for (int q = 0; q < QT; q++) {
-                            const float u = rv[jj * 8 + 2 * q], w = rv[jj * 8 + 2 * q + 1];
+                            for (int q = 0; q < QT; q++) {
+                                const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
 #pragma unroll
-                            for (int i = 0; i < NSI; i++) {
-                                acc[q][i][0] = fmaf(u, ab[i].x, acc[q][i][0]);
-                                acc[q][i][1] = fmaf(u, ab[i].y, acc[q][i][1]);
-                                acc[q][i][2] = fmaf(w, ab[i].y, acc[q][i][2]);
-                                acc[q][i][3] = fmaf(w, ab[i].x, acc[q][i][3]);
+                                for (int i = 0; i < NSI; i++) {
+                                    acc[q][i][0] = fmaf(u, ab[i].x, acc[q][i][0]);
+                                    acc[q][i][1] = fmaf(u, ab[i].y, acc[q][i][1]);
+                                    acc[q][i][2] = fmaf(vv, ab[i].y, acc[q][i][2]);
+                                    acc[q][i][3] = fmaf(vv, ab[i].x, acc[q][i][3]);
+                                }
                             }
                         }
                     }
                 }
-            }
-            __syncthreads(); // staging area read by everyone; previous FFT phase done with zbuf
-            // next group's copies overlap the exchange and the FFT phase
-            if (tid == 0) {
-                unsigned pn = p, sn = s0 + NSI;
-                if (sn >= n_shift) {
-                    pn = p + 1;
-                    sn = 0;
+                tmem_fence_before();
+                __syncthreads(); // staging area read by everyone; previous FFT phase done with zbuf
+                tmem_fence_after();
+                // next copies overlap the exchange and the FFT phase
+                if (tid == 0) {
+                    if (s0 + NSI < n_shift)
+                        issue(grp.sbj_sp, p, s0 + NSI);
+                    else if (p + 1 < pe)
+                        issue(grp.sbj_sp, p + 1, 0);
+                    else if (has_next)
+                        issue(ngrp.sbj_sp, npb, 0);
                 }
-                if (pn < p_end)
-                    issue(pn, sn);
-            }
-            // ---- exchange: half h owns shifts {2h, 2h+1} of the group ----
+                // ---- exchange: half h owns shifts {2h, 2h+1} of the group ----
 #pragma unroll
-            for (int i = 0; i < NSI; i++) {
-                if ((i >> 1) != half) {
+                for (int i = 0; i < NSI; i++) {
+                    if ((i >> 1) != half) {
 #pragma unroll
-                    for (int q = 0; q < QT; q++)
+                        for (int q = 0; q < QT; q++)
 #pragma unroll
-                        for (int c = 0; c < 4; c++)
-                            xbuf[(((half * 8) + (i & 1) * 4 + q) * 4 + c) * kSlots + k] = acc[q][i][c];
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int ii = 0; ii < 2; ii++) {
-                const int i = half * 2 + ii;
-#pragma unroll
-                for (int q = 0; q < QT; q++) {
-                    float s4[4];
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        // compile-time indices on both sides keep acc in registers
-                        const float mine = half ? acc[q][2 + ii][c] : acc[q][ii][c];
-                        s4[c] = mine + xbuf[((((1 - half) * 8) + ii * 4 + q) * 4 + c) * kSlots + k];
+                            for (int c = 0; c < 4; c++)
+                                xbuf[(((half * 8) + (i & 1) * 4 + q) * 4 + c) * kSlots + k] = acc[q][i][c];
                     }
-                    write_z(zbuf + (i * QT + q) * kPairStride, k, s4[0], s4[1], s4[2], s4[3]);
                 }
+                __syncthreads();
+#pragma unroll
+                for (int ii = 0; ii < 2; ii++) {
+                    const int i = half * 2 + ii;
+#pragma unroll
+                    for (int q = 0; q < QT; q++) {
+                        float s4[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            // compile-time indices on both sides keep acc in registers
+                            const float mine = half ? acc[q][2 + ii][c] : acc[q][ii][c];
+                            s4[c] = mine + xbuf[((((1 - half) * 8) + ii * 4 + q) * 4 + c) * kSlots + k];
+                        }
+                        write_z(zbuf + (i * QT + q) * kPairStride, k, s4[0], s4[1], s4[2], s4[3]);
+                    }
+                }
+                __syncthreads();
+                // ---- inverse FFT + peak search, one pair per 16-thread group ----
+                const unsigned s = s0 + g_shift;
+                if (s < n_shift)
+                    fft_peak(gz, tw, l, gmask, s, n_shift, st);
             }
-            __syncthreads();
-            // ---- inverse FFT + peak search, one pair per 16-thread group ----
-            const unsigned s = s0 + g_shift;
-            if (s < n_shift)
-                fft_peak(gz, tw, l, gmask, s, n_shift, st);
+            if (failed)
+                break;
+            merge_write(slots, st, tid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p, grp.p_total, shifts_f,
+                        grp.base, grp.d_out, grp.peak_out);
         }
-        if (failed)
+        if (failed || !has_next)
             break;
-        merge_write(slots, st, tid, g, l, QT, NSI, q0, n_ref, n_shift, p_global0 + p, p_total, shifts_f, base, d_out,
-                    peak_out);
+        item += gridDim.x;
+        grp = ngrp;
+        q0 = nq0;
+        pb = npb;
+        pe = npe;
+        tmem_fence_after();
     }
     if (failed && tid == 0) {
         atomicExch(err, 1u);
@@ -473,14 +522,12 @@ ccf_peak_tmem_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict
 }
 
 // ============================================================================
-// general kernel: references in shared memory, subject spectra in registers
+// general kernel: references in shared memory, subject spectra in registers;
+// persistent over work items
 template <int QT>
 __global__ void __launch_bounds__(256, 1)
-ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ ref_sp,
-                const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift, unsigned n_ref,
-                unsigned n_part, unsigned part_per_cta, unsigned p_global0, unsigned p_total,
-                const float2* __restrict__ shifts_f, const float2* __restrict__ base,
-                float* __restrict__ d_out, float4* __restrict__ peak_out)
+ccf_peak_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift,
+                const float2* __restrict__ shifts_f)
 {
     constexpr int NSI = 16 / QT; // shifts per iteration
     constexpr int RPT = QT / 2;  // references per thread
@@ -497,20 +544,7 @@ ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ re
     const int tid = threadIdx.x;
     const int k = tid & (kSlots - 1);
     const int half = tid >> 7;
-    const unsigned q0 = blockIdx.x * QT;
-
     tw[tid] = twiddle[tid];
-    // reference tile -> shared memory (zero padded rings / missing refs)
-    for (unsigned idx = tid; idx < (unsigned)QT * nrp * kSlots; idx += 256) {
-        unsigned qq = idx / (nrp * kSlots);
-        unsigned rem = idx - qq * nrp * kSlots;
-        unsigned r = rem / kSlots, kk = rem - r * kSlots;
-        float2 v = make_float2(0.f, 0.f);
-        if (q0 + qq < n_ref && r < ring_num)
-            v = __ldg(&ref_sp[((size_t)(q0 + qq) * ring_num + r) * kSlots + kk]);
-        rsp[idx] = v;
-    }
-    __syncthreads();
 
     const int g = tid >> 4, l = tid & 15;
     const unsigned gmask = 0xffffu << (tid & 16);
@@ -518,87 +552,103 @@ ccf_peak_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__ re
     float2* gz = zbuf + g * kPairStride;
     const unsigned n_chunks = nrp / RC;
 
-    for (unsigned pi = 0; pi < part_per_cta; pi++) {
-        const unsigned p = blockIdx.y * part_per_cta + pi;
-        if (p >= n_part)
+    for (unsigned item = blockIdx.x;; item += gridDim.x) {
+        CcfGroup grp;
+        unsigned q0, pb, pe;
+        if (!decode_item(w, item, QT, grp, q0, pb, pe))
             break;
-        PeakState st;
-        st.reset();
+        __syncthreads(); // previous item is done with the reference tile
+        // reference tile -> shared memory (zero padded rings / missing refs)
+        for (unsigned idx = tid; idx < (unsigned)QT * nrp * kSlots; idx += 256) {
+            unsigned qq = idx / (nrp * kSlots);
+            unsigned rem = idx - qq * nrp * kSlots;
+            unsigned r = rem / kSlots, kk = rem - r * kSlots;
+            float2 v = make_float2(0.f, 0.f);
+            if (q0 + qq < grp.n_ref && r < ring_num)
+                v = __ldg(&grp.ref_sp[((size_t)(q0 + qq) * ring_num + r) * kSlots + kk]);
+            rsp[idx] = v;
+        }
+        __syncthreads();
 
-        for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
-            float acc[RPT][NSI][4];
+        for (unsigned p = pb; p < pe; p++) {
+            PeakState st;
+            st.reset();
+            for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
+                float acc[RPT][NSI][4];
 #pragma unroll
-            for (int j = 0; j < RPT; j++)
+                for (int j = 0; j < RPT; j++)
 #pragma unroll
-                for (int i = 0; i < NSI; i++)
+                    for (int i = 0; i < NSI; i++)
 #pragma unroll
-                    for (int c = 0; c < 4; c++)
-                        acc[j][i][c] = 0.f;
+                        for (int c = 0; c < 4; c++)
+                            acc[j][i][c] = 0.f;
 
-            const float2* srow[NSI];
-            bool svalid[NSI];
+                const float2* srow[NSI];
+                bool svalid[NSI];
 #pragma unroll
-            for (int i = 0; i < NSI; i++) {
-                unsigned s = s0 + i;
-                svalid[i] = s < n_shift;
-                srow[i] = sbj_sp + ((size_t)p * n_shift + (svalid[i] ? s : 0)) * ring_num * kSlots + k;
-            }
-            // ring chunks in two register buffers used alternately: the next
-            // chunk's loads are in flight while the current one is consumed
-            float2 bufa[NSI][RC], bufb[NSI][RC];
-            auto load = [&](float2 (&dst)[NSI][RC], unsigned r0) {
+                for (int i = 0; i < NSI; i++) {
+                    unsigned s = s0 + i;
+                    svalid[i] = s < n_shift;
+                    srow[i] = grp.sbj_sp + ((size_t)p * n_shift + (svalid[i] ? s : 0)) * ring_num * kSlots + k;
+                }
+                // ring chunks in two register buffers used alternately: the next
+                // chunk's loads are in flight while the current one is consumed
+                float2 bufa[NSI][RC], bufb[NSI][RC];
+                auto load = [&](float2 (&dst)[NSI][RC], unsigned r0) {
 #pragma unroll
-                for (int i = 0; i < NSI; i++)
+                    for (int i = 0; i < NSI; i++)
 #pragma unroll
-                    for (int rr = 0; rr < RC; rr++)
-                        dst[i][rr] = (svalid[i] && r0 + rr < ring_num) ? __ldg(srow[i] + (size_t)(r0 + rr) * kSlots)
-                                                                       : make_float2(0.f, 0.f);
-            };
-            auto consume = [&](const float2 (&src)[NSI][RC], unsigned r0) {
+                        for (int rr = 0; rr < RC; rr++)
+                            dst[i][rr] = (svalid[i] && r0 + rr < ring_num)
+                                             ? __ldg(srow[i] + (size_t)(r0 + rr) * kSlots)
+                                             : make_float2(0.f, 0.f);
+                };
+                auto consume = [&](const float2 (&src)[NSI][RC], unsigned r0) {
 #pragma unroll
-                for (int j = 0; j < RPT; j++) {
-                    const float2* rq = rsp + ((size_t)(half * RPT + j) * nrp + r0) * kSlots + k;
+                    for (int j = 0; j < RPT; j++) {
+                        const float2* rq = rsp + ((size_t)(half * RPT + j) * nrp + r0) * kSlots + k;
 #pragma unroll
-                    for (int rr = 0; rr < RC; rr++) {
-                        const float2 uv = rq[rr * kSlots];
+                        for (int rr = 0; rr < RC; rr++) {
+                            const float2 uv = rq[rr * kSlots];
 #pragma unroll
-                        for (int i = 0; i < NSI; i++) {
-                            const float2 ab = src[i][rr];
-                            acc[j][i][0] = fmaf(uv.x, ab.x, acc[j][i][0]);
-                            acc[j][i][1] = fmaf(uv.x, ab.y, acc[j][i][1]);
-                            acc[j][i][2] = fmaf(uv.y, ab.y, acc[j][i][2]);
-                            acc[j][i][3] = fmaf(uv.y, ab.x, acc[j][i][3]);
+                            for (int i = 0; i < NSI; i++) {
+                                const float2 ab = src[i][rr];
+                                acc[j][i][0] = fmaf(uv.x, ab.x, acc[j][i][0]);
+                                acc[j][i][1] = fmaf(uv.x, ab.y, acc[j][i][1]);
+                                acc[j][i][2] = fmaf(uv.y, ab.y, acc[j][i][2]);
+                                acc[j][i][3] = fmaf(uv.y, ab.x, acc[j][i][3]);
+                            }
                         }
                     }
+                };
+                load(bufa, 0);
+                for (unsigned c = 0; c < n_chunks; c += 2) {
+                    if (c + 1 < n_chunks)
+                        load(bufb, (c + 1) * RC);
+                    consume(bufa, c * RC);
+                    if (c + 1 < n_chunks) {
+                        if (c + 2 < n_chunks)
+                            load(bufa, (c + 2) * RC);
+                        consume(bufb, (c + 1) * RC);
+                    }
                 }
-            };
-            load(bufa, 0);
-            for (unsigned c = 0; c < n_chunks; c += 2) {
-                if (c + 1 < n_chunks)
-                    load(bufb, (c + 1) * RC);
-                consume(bufa, c * RC);
-                if (c + 1 < n_chunks) {
-                    if (c + 2 < n_chunks)
-                        load(bufa, (c + 2) * RC);
-                    consume(bufb, (c + 1) * RC);
-                }
+
+                __syncthreads(); // previous FFT phase is done with zbuf
+#pragma unroll
+                for (int j = 0; j < RPT; j++)
+#pragma unroll
+                    for (int i = 0; i < NSI; i++)
+                        write_z(zbuf + (i * QT + half * RPT + j) * kPairStride, k, acc[j][i][0], acc[j][i][1],
+                                acc[j][i][2], acc[j][i][3]);
+                __syncthreads();
+
+                const unsigned s = s0 + g_shift;
+                if (s < n_shift)
+                    fft_peak(gz, tw, l, gmask, s, n_shift, st);
             }
-
-            __syncthreads(); // previous FFT phase is done with zbuf
-#pragma unroll
-            for (int j = 0; j < RPT; j++)
-#pragma unroll
-                for (int i = 0; i < NSI; i++)
-                    write_z(zbuf + (i * QT + half * RPT + j) * kPairStride, k, acc[j][i][0], acc[j][i][1],
-                            acc[j][i][2], acc[j][i][3]);
-            __syncthreads();
-
-            const unsigned s = s0 + g_shift;
-            if (s < n_shift)
-                fft_peak(gz, tw, l, gmask, s, n_shift, st);
+            merge_write(slots, st, tid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p, grp.p_total, shifts_f,
+                        grp.base, grp.d_out, grp.peak_out);
         }
-        merge_write(slots, st, tid, g, l, QT, NSI, q0, n_ref, n_shift, p_global0 + p, p_total, shifts_f, base, d_out,
-                    peak_out);
     }
 }
 
@@ -621,6 +671,21 @@ size_t ccf_peak_smem_bytes(unsigned ring_num)
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot);
 }
 
+unsigned ccf_refs_per_item(unsigned ring_num, int variant)
+{
+    if (variant == kCcfTmem && ring_num <= kTmaMaxRings)
+        return 4;
+    return ccf_refs_per_cta(ring_num);
+}
+
+int ccf_variant(unsigned ring_num, bool aligned)
+{
+    // GPUISAC_CCF_KERNEL=general selects the general kernel for every ring count
+    const char* sel = getenv("GPUISAC_CCF_KERNEL");
+    const bool force_general = sel && strcmp(sel, "general") == 0;
+    return (ring_num <= kTmaMaxRings && aligned && !force_general) ? kCcfTmem : kCcfGeneral;
+}
+
 template <typename K>
 static cudaError_t set_max_smem(K kernel)
 {
@@ -630,47 +695,52 @@ static cudaError_t set_max_smem(K kernel)
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin);
 }
 
-template <int QT>
-static cudaError_t launch_qt(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle, unsigned ring_num,
-                             unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_global0,
-                             unsigned p_total, const float2* shifts_f, const float2* base, float* d_out,
-                             float4* peak_out, cudaStream_t stream)
+static unsigned persistent_grid(unsigned n_items, unsigned ctas_per_sm)
 {
-    static int configured = 0;
-    if (!configured) {
-        cudaError_t e = set_max_smem(ccf_peak_kernel<QT>);
-        if (e != cudaSuccess)
-            return e;
-        configured = 1;
-    }
-    const unsigned ref_tiles = (n_ref + QT - 1) / QT;
-    const unsigned ppc = 8;
-    dim3 grid(ref_tiles, (n_part + ppc - 1) / ppc);
-    ccf_peak_kernel<QT><<<grid, 256, ccf_peak_smem_bytes(ring_num), stream>>>(
-        sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, ppc, p_global0, p_total, shifts_f, base, d_out,
-        peak_out);
-    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
-    return cudaGetLastError();
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned cap = (unsigned)std::max(sms, 1) * std::max(ctas_per_sm, 1u);
+    return std::max(1u, std::min(n_items, cap));
 }
 
-static cudaError_t launch_tmem(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle, unsigned ring_num,
-                               unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_global0,
-                               unsigned p_total, const float2* shifts_f, const float2* base, float* d_out,
-                               float4* peak_out, unsigned* err, cudaStream_t stream)
+cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* twiddle, unsigned ring_num,
+                                 unsigned n_shift, const float2* shifts_f, unsigned* err, cudaStream_t stream)
 {
-    static int configured = 0;
-    if (!configured) {
-        cudaError_t e = set_max_smem(ccf_peak_tmem_kernel);
-        if (e != cudaSuccess)
-            return e;
-        configured = 1;
+    if (w.n_items == 0)
+        return cudaSuccess;
+    const unsigned grid = persistent_grid(w.n_items, 1);
+    if (variant == kCcfTmem) {
+        static int configured = 0;
+        if (!configured) {
+            cudaError_t e = set_max_smem(ccf_peak_tmem_kernel);
+            if (e != cudaSuccess)
+                return e;
+            configured = 1;
+        }
+        ccf_peak_tmem_kernel<<<grid, 256, tma_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift, shifts_f,
+                                                                              err);
+    } else if (ccf_refs_per_cta(ring_num) == 4) {
+        static int configured = 0;
+        if (!configured) {
+            cudaError_t e = set_max_smem(ccf_peak_kernel<4>);
+            if (e != cudaSuccess)
+                return e;
+            configured = 1;
+        }
+        ccf_peak_kernel<4><<<grid, 256, ccf_peak_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift,
+                                                                               shifts_f);
+    } else {
+        static int configured = 0;
+        if (!configured) {
+            cudaError_t e = set_max_smem(ccf_peak_kernel<2>);
+            if (e != cudaSuccess)
+                return e;
+            configured = 1;
+        }
+        ccf_peak_kernel<2><<<grid, 256, ccf_peak_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift,
+                                                                               shifts_f);
     }
-    const unsigned ref_tiles = (n_ref + 3) / 4;
-    const unsigned ppc = 8;
-    dim3 grid(ref_tiles, (n_part + ppc - 1) / ppc);
-    ccf_peak_tmem_kernel<<<grid, 256, tma_smem_bytes(ring_num), stream>>>(
-        sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, ppc, p_global0, p_total, shifts_f, base, d_out,
-        peak_out, err);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }
@@ -682,19 +752,28 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
 {
     if (n_part == 0 || n_ref == 0)
         return cudaSuccess;
-    // GPUISAC_CCF_KERNEL=general selects the general kernel for every ring count
-    const char* sel = getenv("GPUISAC_CCF_KERNEL");
-    const bool force_general = sel && strcmp(sel, "general") == 0;
     // bulk copies need 16-byte aligned sources (every row is a multiple of 1 KiB)
-    const bool aligned = ((uintptr_t)sbj_sp & 15) == 0;
-    if (ring_num <= kTmaMaxRings && err && aligned && !force_general)
-        return launch_tmem(sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, p_global0, p_total, shifts_f,
-                           base, d_out, peak_out, err, stream);
-    if (ccf_refs_per_cta(ring_num) == 4)
-        return launch_qt<4>(sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, p_global0, p_total, shifts_f,
-                            base, d_out, peak_out, stream);
-    return launch_qt<2>(sbj_sp, ref_sp, twiddle, ring_num, n_shift, n_ref, n_part, p_global0, p_total, shifts_f, base,
-                        d_out, peak_out, stream);
+    const bool aligned = ((uintptr_t)sbj_sp & 15) == 0 && err != nullptr;
+    const int variant = ccf_variant(ring_num, aligned);
+    const unsigned qt = ccf_refs_per_item(ring_num, variant);
+    CcfWork w{};
+    w.groups = nullptr;
+    w.n_groups = 1;
+    w.ppc = kCcfParticlesPerItem;
+    CcfGroup& g = w.one;
+    g.sbj_sp = sbj_sp;
+    g.ref_sp = ref_sp;
+    g.base = base;
+    g.d_out = d_out;
+    g.peak_out = peak_out;
+    g.p_first = p_global0;
+    g.n_part = n_part;
+    g.n_ref = n_ref;
+    g.p_total = p_total;
+    g.item_begin = 0;
+    g.ref_tiles = (n_ref + qt - 1) / qt;
+    w.n_items = g.ref_tiles * ((n_part + w.ppc - 1) / w.ppc);
+    return launch_ccf_peak_work(w, variant, twiddle, ring_num, n_shift, shifts_f, err, stream);
 }
 
 } // namespace gpuisac

@@ -42,6 +42,44 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
 // whose spectra are in sbj_sp ([n_part][n_shift][ring_num][kSlots]); results
 // for particle i go to column p_global0 + i of d_out [n_ref][p_total] and
 // peak_out [n_ref][p_total] (angle, shift_x, shift_y, mirror).
+// One alignment group as the CCF / peak kernels see it: the particles of the
+// group present in the current spectra buffer against all its references.
+struct CcfGroup {
+    const float2* sbj_sp;   // [n_part][n_shift][ring_num][kSlots]
+    const float2* ref_sp;   // [n_ref][ring_num][kSlots]
+    const float2* base;     // base shifts, indexed by the particle's index in the group; or null
+    float* d_out;           // [n_ref][p_total]
+    float4* peak_out;       // [n_ref][p_total]
+    unsigned p_first;       // index in the group of sbj_sp's first particle
+    unsigned n_part;        // particles of the group in sbj_sp
+    unsigned n_ref;         // references of the group
+    unsigned p_total;       // particles in the group (row pitch of the outputs)
+    unsigned item_begin;    // first work item of the group
+    unsigned ref_tiles;     // reference tiles of the group
+};
+
+// Work of one CCF launch: either one group (groups == null, `one`) or a
+// device table of n_groups groups ordered by item_begin.
+struct CcfWork {
+    const CcfGroup* groups;
+    CcfGroup one;
+    unsigned n_groups;
+    unsigned n_items;
+    unsigned ppc; // particles per work item
+};
+
+enum { kCcfGeneral = 0, kCcfTmem = 1 };
+constexpr unsigned kCcfParticlesPerItem = 8;
+
+// kernel variant for a ring count (aligned: spectra rows 16-byte aligned)
+int ccf_variant(unsigned ring_num, bool aligned);
+// references per work item of that variant
+unsigned ccf_refs_per_item(unsigned ring_num, int variant);
+
+// persistent launch over the work items of w
+cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* twiddle, unsigned ring_num,
+                                 unsigned n_shift, const float2* shifts_f, unsigned* err, cudaStream_t stream);
+
 // err: device word set to non-zero if a kernel gave up waiting for its own
 // asynchronous copies (bounded waits; the host checks it after the stream).
 cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle,

@@ -23,6 +23,9 @@ struct HostGeometry {
 // failure) and fills the host tables.  Returns 0 or an error code.
 int host_geometry(const AlignConfig* cfg, HostGeometry& out);
 
+// The reference's subject batch size for cfg (its sbj_num / ref_num).
+unsigned reference_batch(const AlignConfig* cfg);
+
 // Images of side dim per 2D linear texture on device dev.
 unsigned texture_images(int dev, unsigned dim);
 

@@ -42,8 +42,14 @@ EXPORTS = (
     "ref_free_alignment_2D_filter_references", "gpuisac_last_error", "gpuisac_clear_error",
     "gpuisac_version", "gpuisac_multi_ref_align_device", "gpuisac_spectra_device", "gpuisac_spectra_device_layout",
     "gpuisac_ccf_peak_device", "gpuisac_shift_count", "gpuisac_launch_count", "gpuisac_profile",
-    "gpuisac_kernel_time", "gpuisac_multi_ref_align_device_noalloc",
+    "gpuisac_kernel_time", "gpuisac_multi_ref_align_device_noalloc", "gpuisac_multi_ref_align_groups_device",
 )
+
+
+class GpuisacGroup(ctypes.Structure):
+    """Mirror of GpuisacGroup (include/gpu_aln_pack.h)."""
+    _fields_ = [("sbj_offset", ctypes.c_uint), ("sbj_num", ctypes.c_uint), ("ref_offset", ctypes.c_uint),
+                ("ref_num", ctypes.c_uint), ("out_offset", ctypes.c_ulonglong)]
 
 
 class GpuIsacError(RuntimeError):
@@ -89,6 +95,10 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                          ctypes.c_void_p]
     L.gpuisac_multi_ref_align_device_noalloc.restype = ctypes.c_int
+    L.gpuisac_multi_ref_align_groups_device.argtypes = [aln_cfg_ptr, ctypes.POINTER(GpuisacGroup), ctypes.c_uint,
+                                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.gpuisac_multi_ref_align_groups_device.restype = ctypes.c_int
     L.gpuisac_spectra_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.gpuisac_spectra_device.restype = ctypes.c_int

@@ -129,3 +129,44 @@ def peak_tuples(peak_list: np.ndarray) -> np.ndarray:
     """[ref][4*sbj] -> [ref][sbj][4]"""
     R = peak_list.shape[0]
     return peak_list.reshape(R, -1, 4)
+
+
+def multi_ref_align_groups_device(particles, refs, groups, ring_num: int, shift_rng_x: float, shift_rng_y: float,
+                                  shift_step: float = 1.0, base_shifts=None, stream=None):
+    """Many independent groups in one pass (gpuisac_multi_ref_align_groups_device).
+
+    particles, refs: CUDA tensors [n][D][D]; groups: list of
+    (sbj_offset, sbj_num, ref_offset, ref_num).  Returns (d, peak, offsets):
+    flat result tensors and each group's element offset; group i's results are
+    d[off:off+R*P].view(R, P) and peak[off:off+R*P].view(R, P, 4).
+    """
+    import torch
+
+    from ._lib import GpuisacGroup
+
+    particles = particles.contiguous().float()
+    refs = refs.contiguous().float()
+    P, D = particles.shape[0], particles.shape[1]
+    R = refs.shape[0]
+    cfg = make_config(P, R, D, ring_num, 256, shift_step, shift_rng_x, shift_rng_y)
+    tbl = (GpuisacGroup * max(len(groups), 1))()
+    offsets, off = [], 0
+    for i, (so, sn, ro, rn) in enumerate(groups):
+        tbl[i] = GpuisacGroup(so, sn, ro, rn, off)
+        offsets.append(off)
+        off += sn * rn
+    d = torch.empty(max(off, 1), dtype=torch.float32, device=particles.device)
+    pk = torch.empty((max(off, 1), 4), dtype=torch.float32, device=particles.device)
+    base_ptr = None
+    if base_shifts is not None:
+        base_shifts = base_shifts.contiguous().float()
+        base_ptr = base_shifts.data_ptr()
+    st = stream if stream is not None else torch.cuda.current_stream(particles.device)
+    L = _lib.load()
+    rc = L.gpuisac_multi_ref_align_groups_device(ctypes.byref(cfg), tbl, len(groups), particles.data_ptr(),
+                                                 refs.data_ptr(), base_ptr, d.data_ptr(), pk.data_ptr(),
+                                                 st.cuda_stream)
+    if rc:
+        _lib.check(L)
+        raise GpuIsacError(f"gpuisac_multi_ref_align_groups_device failed ({rc})")
+    return d, pk, offsets

@@ -139,6 +139,31 @@ int gpuisac_multi_ref_align_device_noalloc(const AlignConfig *cfg, const float *
                                            const float *base_shift, float *d_out, float *peak_out,
                                            void *stream);
 
+/* One independent alignment group of gpuisac_multi_ref_align_groups_device. */
+typedef struct GpuisacGroup {
+    unsigned int sbj_offset;       /* first particle of the group in the subject stack */
+    unsigned int sbj_num;          /* its particles */
+    unsigned int ref_offset;       /* first reference of the group in the reference stack */
+    unsigned int ref_num;          /* its references */
+    unsigned long long out_offset; /* element offset of its [ref_num][sbj_num] block in d_out
+                                      (and of its [ref_num][sbj_num][4] block in peak_out) */
+} GpuisacGroup;
+
+/* No single counterpart in the reference, which aligns one group per
+ * multi_ref_align_init / multi_ref_align / gpu_clear cycle
+ * (bin/sp_isac2_gpu.py:937-1032).  Aligns n_groups independent groups --
+ * each group's particles against its own references -- in one pass over
+ * device stacks: cfg gives the shared geometry (img_dim, ring_num, ring_len,
+ * shift grid) and, in sbj_num / ref_num, the stack sizes.  Each group's
+ * results equal those of a separate alignment of that group.  The launch
+ * sequence is recorded in a CUDA graph and replayed when the identical call
+ * (same groups, pointers, stream) is made again.  Blocks until done.
+ * Returns 0 or an error code. */
+int gpuisac_multi_ref_align_groups_device(const AlignConfig *cfg, const GpuisacGroup *groups,
+                                          unsigned int n_groups, const float *sbj, const float *ref,
+                                          const float *base_shift, float *d_out, float *peak_out,
+                                          void *stream);
+
 /* Ring spectra of a device image stack at every shift of cfg's grid, as the
  * CCF kernel consumes them: out [n_img][n_shift][ring_num][128][2] (float),
  * slot 0 = (F[0], F[128]); is_ref selects the reference layout (ring weight
