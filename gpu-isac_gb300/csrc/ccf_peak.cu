@@ -284,6 +284,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 }
 } // namespace
 
+// spectra row of the group's q-th reference
+__device__ __forceinline__ unsigned ref_row(const CcfGroup& g, unsigned q) { return g.ref_idx ? g.ref_idx[q] : q; }
+
 // ---- work items ----
 // Work item = (group, reference tile, block of up to ppc particles).  Items of
 // a group are numbered reference tile fastest, so consecutive items (running
@@ -393,7 +396,7 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
             for (int q = 0; q < QT; q++) {
                 float2 uv = make_float2(0.f, 0.f);
                 if (j < rh && q0 + q < grp.n_ref)
-                    uv = __ldg(&grp.ref_sp[((size_t)(q0 + q) * ring_num + r_base + j) * kSlots + k]);
+                    uv = __ldg(&grp.ref_sp[((size_t)ref_row(grp, q0 + q) * ring_num + r_base + j) * kSlots + k]);
                 v[2 * q] = uv.x;
                 v[2 * q + 1] = uv.y;
             }
@@ -565,7 +568,7 @@ ccf_peak_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num
             unsigned r = rem / kSlots, kk = rem - r * kSlots;
             float2 v = make_float2(0.f, 0.f);
             if (q0 + qq < grp.n_ref && r < ring_num)
-                v = __ldg(&grp.ref_sp[((size_t)(q0 + qq) * ring_num + r) * kSlots + kk]);
+                v = __ldg(&grp.ref_sp[((size_t)ref_row(grp, q0 + qq) * ring_num + r) * kSlots + kk]);
             rsp[idx] = v;
         }
         __syncthreads();

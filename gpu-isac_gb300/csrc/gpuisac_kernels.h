@@ -31,12 +31,14 @@ size_t ccf_peak_smem_bytes(unsigned ring_num);
 // kernels launched by this library since load (all launchers count here)
 extern std::atomic<unsigned long long> g_kernel_launches;
 
-// Resample + normalise + ring FFT of n_img images x n_shift shifts.
-// out: [n_img][n_shift][ring_num][kSlots] float2 (see polar_spectra.cu).
+// Resample + normalise + ring FFT of n_img images x n_shift shifts: images
+// img0 .. img0 + n_img - 1 of the stack, or img_list[0 .. n_img-1] (device)
+// when a list is given.  out: [n_img][n_shift][ring_num][kSlots] float2
+// (see polar_spectra.cu).
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,
                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
-                                 float2* out, cudaStream_t stream);
+                                 float2* out, cudaStream_t stream, const unsigned* img_list = nullptr);
 
 // CCF against every reference + inverse FFT + peak search for n_part particles
 // whose spectra are in sbj_sp ([n_part][n_shift][ring_num][kSlots]); results
@@ -56,6 +58,7 @@ struct CcfGroup {
     unsigned p_total;       // particles in the group (row pitch of the outputs)
     unsigned item_begin;    // first work item of the group
     unsigned ref_tiles;     // reference tiles of the group
+    const unsigned* ref_idx; // rows of ref_sp holding the group's references 0..n_ref-1; null = 0..n_ref-1
 };
 
 // Work of one CCF launch: either one group (groups == null, `one`) or a

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(256)
 polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
                      unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
                      const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
-                     float2* __restrict__ out)
+                     float2* __restrict__ out, const unsigned* __restrict__ img_list)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* polar = reinterpret_cast<float*>(smem_raw);                        // [ring_num][256]
@@ -37,7 +37,8 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
     const unsigned s = row - img_local * n_shift;
     if (img_local >= n_img)
         return;
-    const unsigned img = img0 + img_local;
+    // output row i holds image img0 + i, or img_list[i] when a list is given
+    const unsigned img = img_list ? img_list[img_local] : img0 + img_local;
     const int tid = threadIdx.x;
 
     tw[tid] = twiddle[tid];
@@ -143,7 +144,7 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,
                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
-                                 float2* out, cudaStream_t stream)
+                                 float2* out, cudaStream_t stream, const unsigned* img_list)
 {
     if (n_img == 0 || n_shift == 0)
         return cudaSuccess;
@@ -158,7 +159,7 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
     }
     unsigned rows = n_img * n_shift;
     polar_spectra_kernel<<<rows, 256, smem, stream>>>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base,
-                                                       img0, n_img, is_ref, out);
+                                                       img0, n_img, is_ref, out, img_list);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

@@ -43,6 +43,10 @@ EXPORTS = (
     "gpuisac_version", "gpuisac_multi_ref_align_device", "gpuisac_spectra_device", "gpuisac_spectra_device_layout",
     "gpuisac_ccf_peak_device", "gpuisac_shift_count", "gpuisac_launch_count", "gpuisac_profile",
     "gpuisac_kernel_time", "gpuisac_multi_ref_align_device_noalloc", "gpuisac_multi_ref_align_groups_device",
+    "gpuisac_align_proposals_device", "gpuisac_nn_features", "gpuisac_nn_gemm", "gpuisac_nn_bias_act",
+    "gpuisac_nn_relu_backward", "gpuisac_nn_colsum", "gpuisac_nn_l2norm", "gpuisac_nn_l2norm_backward",
+    "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
+    "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device",
 )
 
 
@@ -50,6 +54,13 @@ class GpuisacGroup(ctypes.Structure):
     """Mirror of GpuisacGroup (include/gpu_aln_pack.h)."""
     _fields_ = [("sbj_offset", ctypes.c_uint), ("sbj_num", ctypes.c_uint), ("ref_offset", ctypes.c_uint),
                 ("ref_num", ctypes.c_uint), ("out_offset", ctypes.c_ulonglong)]
+
+
+class GpuisacProposalNet(ctypes.Structure):
+    """Mirror of GpuisacProposalNet (include/gpu_aln_pack.h): device pointers."""
+    _fields_ = [("nk", ctypes.c_uint), ("hidden", ctypes.c_uint), ("emb", ctypes.c_uint),
+                ("mu", ctypes.c_void_p), ("inv_sd", ctypes.c_void_p), ("W1", ctypes.c_void_p),
+                ("b1", ctypes.c_void_p), ("W2", ctypes.c_void_p), ("b2", ctypes.c_void_p)]
 
 
 class GpuIsacError(RuntimeError):
@@ -99,6 +110,28 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.gpuisac_multi_ref_align_groups_device.restype = ctypes.c_int
+    vp, ci, cl, cf, cu = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_float, ctypes.c_uint
+    L.gpuisac_align_proposals_device.argtypes = [aln_cfg_ptr, vp, vp, vp, vp, cu, vp, cu, vp, vp, vp]
+    L.gpuisac_nn_features.argtypes = [vp, cu, cu, cu, vp, vp, vp, vp]
+    L.gpuisac_nn_col_stats.argtypes = [vp, cl, ci, cf, vp, vp, vp]
+    L.gpuisac_nn_affine_cols.argtypes = [vp, cl, ci, vp, vp, vp]
+    L.gpuisac_nn_group_max.argtypes = [vp, cl, ci, ci, vp, vp]
+    L.gpuisac_learned_align_device.argtypes = [aln_cfg_ptr, vp, vp, vp, ctypes.POINTER(GpuisacProposalNet), vp, cu,
+                                               cf, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_ulonglong), vp]
+    L.gpuisac_nn_gemm.argtypes = [ci, ci, ci, cf, vp, cl, cl, vp, cl, cl, cf, vp, cl, vp]
+    L.gpuisac_nn_bias_act.argtypes = [vp, vp, cl, ci, ci, vp]
+    L.gpuisac_nn_relu_backward.argtypes = [vp, vp, cl, vp]
+    L.gpuisac_nn_colsum.argtypes = [vp, cl, ci, vp, ci, vp]
+    L.gpuisac_nn_l2norm.argtypes = [vp, cl, ci, vp, vp, vp]
+    L.gpuisac_nn_l2norm_backward.argtypes = [vp, vp, vp, cl, ci, vp, vp]
+    L.gpuisac_nn_softmax_xent.argtypes = [vp, vp, cl, ci, vp, vp, vp]
+    L.gpuisac_nn_adam.argtypes = [vp, vp, vp, vp, cl, cf, cf, cf, cf, cf, ci, vp]
+    L.gpuisac_nn_topk.argtypes = [vp, cl, ci, ci, vp, vp]
+    for name in ("gpuisac_align_proposals_device", "gpuisac_nn_features", "gpuisac_nn_gemm", "gpuisac_nn_bias_act",
+                 "gpuisac_nn_relu_backward", "gpuisac_nn_colsum", "gpuisac_nn_l2norm", "gpuisac_nn_l2norm_backward",
+                 "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
+                 "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device"):
+        getattr(L, name).restype = ci
     L.gpuisac_spectra_device.argtypes = [aln_cfg_ptr, ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.gpuisac_spectra_device.restype = ctypes.c_int

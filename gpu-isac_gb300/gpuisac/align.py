@@ -170,3 +170,48 @@ def multi_ref_align_groups_device(particles, refs, groups, ring_num: int, shift_
         _lib.check(L)
         raise GpuIsacError(f"gpuisac_multi_ref_align_groups_device failed ({rc})")
     return d, pk, offsets
+
+
+def align_proposals_device(particles, refs, proposals, ring_num: int, shift_rng_x: float, shift_rng_y: float,
+                           shift_step: float = 1.0, part_idx=None, base_shifts=None, stream=None):
+    """Search selected particles against their own reference lists
+    (gpuisac_align_proposals_device).
+
+    particles, refs: CUDA tensors [n][D][D] (the whole stacks); proposals:
+    int32 CUDA tensor [n_sel][k] of reference indices; part_idx: int32 CUDA
+    tensor [n_sel] of particle indices (None: every particle, in order).
+    Returns (d [n_sel][k], peak [n_sel][k][4]); entry (i, j) equals the full
+    alignment's entry for (reference proposals[i][j], particle part_idx[i]).
+    """
+    import torch
+
+    particles = particles.contiguous().float()
+    refs = refs.contiguous().float()
+    proposals = proposals.contiguous()
+    if proposals.dtype != torch.int32 or proposals.dim() != 2:
+        raise ValueError("proposals must be an int32 [n_sel][k] tensor")
+    P, D = particles.shape[0], particles.shape[1]
+    R = refs.shape[0]
+    n_sel, k = proposals.shape
+    idx_ptr = None
+    if part_idx is not None:
+        part_idx = part_idx.contiguous()
+        if part_idx.dtype != torch.int32 or part_idx.numel() != n_sel:
+            raise ValueError("part_idx must be an int32 tensor with one entry per proposal row")
+        idx_ptr = part_idx.data_ptr()
+    cfg = make_config(P, R, D, ring_num, 256, shift_step, shift_rng_x, shift_rng_y)
+    d = torch.empty((n_sel, k), dtype=torch.float32, device=particles.device)
+    pk = torch.empty((n_sel, k, 4), dtype=torch.float32, device=particles.device)
+    base_ptr = None
+    if base_shifts is not None:
+        base_shifts = base_shifts.contiguous().float()
+        base_ptr = base_shifts.data_ptr()
+    st = stream if stream is not None else torch.cuda.current_stream(particles.device)
+    L = _lib.load()
+    rc = L.gpuisac_align_proposals_device(ctypes.byref(cfg), particles.data_ptr(), refs.data_ptr(), base_ptr,
+                                          idx_ptr, n_sel, proposals.data_ptr(), k, d.data_ptr(), pk.data_ptr(),
+                                          st.cuda_stream)
+    if rc:
+        _lib.check(L)
+        raise GpuIsacError(f"gpuisac_align_proposals_device failed ({rc})")
+    return d, pk

@@ -38,6 +38,7 @@ class Workload:
 WORKLOADS = {
     0: Workload("cpu_2000x64_16ref", 2000, 64, 16, 29, 2, 0.1, 28.0),
     1: Workload("mref_50000x76_200ref", 50000, 76, 200, 35, 3, 0.05, 34.0),
+    3: Workload("learned_100000x76_500ref", 100000, 76, 500, 35, 3, 0.05, 34.0),
     4: Workload("largebox_200000x128_500ref", 200000, 128, 500, 61, 4, 0.03, 60.0),
 }
 
@@ -93,11 +94,15 @@ def _normalise(imgs, mask):
 
 
 def make_stack(n_particles, img_dim, n_classes, shift_rng, snr, blob_radius, seed,
-               mask_radius=None, mirror_p=0.5) -> Stack:
+               mask_radius=None, mirror_p=0.5, particle_seed=None) -> Stack:
+    """particle_seed: draw the particles from their own stream (same class
+    phantoms as `seed`, independent particles: training / held-out splits)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     amp, sig, cx, cy = _blobs(rng, n_classes, blob_radius)
     mask = _mask(img_dim, mask_radius if mask_radius is not None else blob_radius)
     refs = _normalise(_render(amp, sig, cx, cy, img_dim), mask)
+    if particle_seed is not None:
+        rng = np.random.Generator(np.random.PCG64(particle_seed))
 
     cls = rng.integers(0, n_classes, size=n_particles).astype(np.int32)
     ang = rng.uniform(0.0, 360.0, size=n_particles).astype(np.float32)
@@ -122,7 +127,12 @@ def make_stack(n_particles, img_dim, n_classes, shift_rng, snr, blob_radius, see
     return Stack(parts, refs, cls, ang, sh, mir, seed)
 
 
-def workload_stack(idx: int, n_particles: int | None = None, n_refs: int | None = None) -> Stack:
+def workload_stack(idx: int, n_particles: int | None = None, n_refs: int | None = None,
+                   split: int | None = None) -> Stack:
+    """split: None for the workload's own particles; k >= 1 for an independent
+    particle set over the same references (k = 1: the training set of the
+    learned proposal)."""
     w = WORKLOADS[idx]
+    ps = None if split is None else SEED_BASE + 1000 * split + idx
     return make_stack(n_particles or w.n_particles, w.img_dim, n_refs or w.n_classes,
-                      w.shift_rng, w.snr, w.blob_radius, SEED_BASE + idx)
+                      w.shift_rng, w.snr, w.blob_radius, SEED_BASE + idx, particle_seed=ps)

@@ -164,6 +164,98 @@ int gpuisac_multi_ref_align_groups_device(const AlignConfig *cfg, const GpuisacG
                                           const float *base_shift, float *d_out, float *peak_out,
                                           void *stream);
 
+/* No counterpart in the reference.  The exhaustive shift x angle x mirror
+ * search of selected particles against k references each: particle
+ * part_idx[i] (i < n_sel; NULL selects particles 0..sbj_num-1 and n_sel must
+ * be sbj_num) against references proposals[i*k .. i*k+k-1] (device arrays of
+ * reference indices < ref_num).  Writes d_out[i*k + j] and
+ * peak_out[(i*k + j)*4 ..]; each entry equals the one a full
+ * gpuisac_multi_ref_align_device of the same stacks gives for that
+ * (reference, particle).  Used with proposed reference lists, and with every
+ * reference for particles that fall back to the full search.  Blocks until
+ * done.  Returns 0 or an error code. */
+int gpuisac_align_proposals_device(const AlignConfig *cfg, const float *sbj, const float *ref,
+                                   const float *base_shift, const unsigned int *part_idx, unsigned int n_sel,
+                                   const unsigned int *proposals, unsigned int k, float *d_out, float *peak_out,
+                                   void *stream);
+
+/* No counterpart in the reference.  A trained proposal network, as the
+ * learned search reads it (device arrays, row-major FP32). */
+typedef struct GpuisacProposalNet {
+    unsigned int nk;     /* harmonics per ring: ring_num * nk network inputs */
+    unsigned int hidden; /* hidden width */
+    unsigned int emb;    /* embedding width */
+    const float *mu;     /* [ring_num*nk] feature standardisation */
+    const float *inv_sd; /* [ring_num*nk] */
+    const float *W1;     /* [hidden][ring_num*nk] */
+    const float *b1;     /* [hidden] */
+    const float *W2;     /* [emb][hidden] */
+    const float *b2;     /* [emb] */
+} GpuisacProposalNet;
+
+/* No counterpart in the reference.  Best reference and alignment of every
+ * particle by the learned search: the particle's ring spectra at every shift
+ * of cfg's grid feed the network, each reference is scored by the best
+ * cosine similarity over shifts between the particle's embedding and
+ * ref_emb[ref] ([ref_num][emb], unit rows), the top k references are searched
+ * exhaustively (shift x angle x mirror, as the full search does), and a
+ * particle whose best proposed peak beats the runner-up proposal by less
+ * than gap_margin is searched against every reference.  Outputs per particle
+ * p: best_ref[p], best_peak[p], best_param[p*4 ..] (angle, sx, sy, mirror,
+ * as the full search reports them); optional best_gap[p] (best minus
+ * runner-up proposed peak, +inf for k = 1) and fallback[p] (1 if searched
+ * against every reference).  *pairs (optional, host) receives the number of
+ * particle x reference alignments run.  A result equals the full search's
+ * entry for the reference it names; ties go to the smaller reference index.
+ * Blocks until done.  Returns 0 or an error code. */
+int gpuisac_learned_align_device(const AlignConfig *cfg, const float *sbj, const float *ref, const float *base_shift,
+                                 const GpuisacProposalNet *net, const float *ref_emb, unsigned int k,
+                                 float gap_margin, int *best_ref, float *best_peak, float *best_param,
+                                 float *best_gap, unsigned int *fallback, unsigned long long *pairs, void *stream);
+
+/* ---- learned reference proposal (no counterpart in the reference): kernels
+ * of a small embedding network, all on caller-owned row-major FP32 device
+ * arrays, asynchronous on `stream`; each returns 0, or 2 for bad arguments,
+ * 1 for a launch error ---- */
+
+/* feat[i][r*nk + k] = log(1 + |F_r[k]|), k < nk, rows scaled to unit L2 norm,
+ * then standardised per column ((v - mu) * inv_sd) when mu and inv_sd are
+ * given, from spectra rows [n][ring_num][128][2] made by
+ * gpuisac_spectra_device (subject basis): rotation- and mirror-invariant
+ * ring features. */
+int gpuisac_nn_features(const float *spectra, unsigned int n, unsigned int ring_num, unsigned int nk,
+                        const float *mu, const float *inv_sd, float *feat, void *stream);
+/* per-column mean and 1/sqrt(variance + eps) of X [rows][cols]. */
+int gpuisac_nn_col_stats(const float *X, long rows, int cols, float eps, float *mean, float *inv_sd, void *stream);
+/* X[i][j] = (X[i][j] - mu[j]) * inv_sd[j]. */
+int gpuisac_nn_affine_cols(float *X, long rows, int cols, const float *mu, const float *inv_sd, void *stream);
+/* out[i][j] = max over s < group of G[i*group + s][j]. */
+int gpuisac_nn_group_max(const float *G, long n, int group, int cols, float *out, void *stream);
+/* C = alpha * op(A) op(B) + beta * C; A(m,k) at A[m*sam + k*sak], B(k,n) at
+ * B[k*sbk + n*sbn], C row pitch ldc. */
+int gpuisac_nn_gemm(int M, int N, int K, float alpha, const float *A, long sam, long sak, const float *B, long sbk,
+                    long sbn, float beta, float *C, long ldc, void *stream);
+/* Y[i][j] += b[j], then ReLU if relu != 0. */
+int gpuisac_nn_bias_act(float *Y, const float *b, long rows, int cols, int relu, void *stream);
+/* dY[i] = 0 where Y[i] <= 0. */
+int gpuisac_nn_relu_backward(float *dY, const float *Y, long n, void *stream);
+/* db[j] = sum_i dY[i][j], added to db when accumulate != 0. */
+int gpuisac_nn_colsum(const float *dY, long rows, int cols, float *db, int accumulate, void *stream);
+/* E[i] = X[i] / |X[i]|, norm[i] = |X[i]|. */
+int gpuisac_nn_l2norm(const float *X, long rows, int cols, float *E, float *norm, void *stream);
+/* gradient of the row normalisation: dX = (dE - E (E . dE)) / norm. */
+int gpuisac_nn_l2norm_backward(const float *E, const float *dE, const float *norm, long rows, int cols, float *dX,
+                               void *stream);
+/* loss[i] = -log softmax(S[i])[labels[i]]; if dS is given,
+ * dS = (softmax - onehot) / rows (gradient of the mean loss). */
+int gpuisac_nn_softmax_xent(const float *S, const int *labels, long rows, int cols, float *loss, float *dS,
+                            void *stream);
+/* AdamW step (bias-corrected, step >= 1) on n parameters. */
+int gpuisac_nn_adam(float *p, const float *g, float *m, float *v, long n, float lr, float b1, float b2, float eps,
+                    float wd, int step, void *stream);
+/* idx[i][0..k-1] = columns of the k largest S[i][.], best first (cols <= 1024, k <= 64). */
+int gpuisac_nn_topk(const float *S, long rows, int cols, int k, unsigned int *idx, void *stream);
+
 /* Ring spectra of a device image stack at every shift of cfg's grid, as the
  * CCF kernel consumes them: out [n_img][n_shift][ring_num][128][2] (float),
  * slot 0 = (F[0], F[128]); is_ref selects the reference layout (ring weight
