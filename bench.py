@@ -65,6 +65,11 @@ def peaks():
     return FALLBACK_HBM_GBS, FALLBACK_BF16_TFLOPS, "fallback"
 
 
+def fp32_nominal_tflops(sm_mhz: float = 2070.0) -> float:
+    """nominal FP32 FMA rate of a GB300 (152 SMs x 128 FP32 lanes x 2 flops)"""
+    return 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -198,6 +203,113 @@ def bench_reference(args):
     print(json.dumps(line), flush=True)
 
 
+LEARNED = dict(workload="learned_100000x76_500ref", particles=100000, refs=500, train_alignments=200000,
+               img_dim=76, rings=35, shift_range=3, n_shifts=49, snr=0.05, k=32, max_wrong=3e-3)
+
+
+def bench_learned(args, dev, L):
+    """The learned search against the plain FP32 full search on the learned
+    workload: 100,000 held-out particles x 500 references, the network
+    trained (untimed) on 200,000 particles the full search labelled.  Both
+    timed with CUDA events on the same resident inputs; throughput counts
+    particle x reference pairs covered (P x R) per second."""
+    import torch
+
+    from gpuisac import learned, synth
+    from gpuisac.align import multi_ref_align_device
+    w = LEARNED
+    P = args.learned_particles
+    n_train = args.learned_train
+    R, NR, s = w["refs"], w["rings"], float(w["shift_range"])
+    t0 = time.perf_counter()
+    tr = synth.workload_stack(3, n_particles=n_train, n_refs=R, split=1)
+    ev = synth.workload_stack(3, n_particles=P, n_refs=R)
+    t_gen = time.perf_counter() - t0
+    refs = torch.from_numpy(tr.refs).to(dev)
+    tp = torch.from_numpy(tr.particles).to(dev)
+    ep = torch.from_numpy(ev.particles).to(dev)
+    del tr, ev
+    t0 = time.perf_counter()
+    d_tr, pk_tr = multi_ref_align_device(tp, refs, NR, s, s)
+    net = learned.ProposalNet(NR, device=dev, seed=11)
+    rep = learned.train_from_full_search(net, tp, refs, d_tr, pk_tr, NR, s, s, k=w["k"], calib_frac=0.1,
+                                         max_wrong=w["max_wrong"])
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del d_tr, pk_tr, tp
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, warm, steps):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = None
+        for _ in range(steps):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1) / steps
+
+    launches0 = L.gpuisac_launch_count()
+    res, ms_l = timed(lambda: learned.learned_align(ep, refs, net, NR, s, s, k=w["k"], gap_margin=rep.gap_margin),
+                      args.warmup, args.steps)
+    launches = (L.gpuisac_launch_count() - launches0) // (args.warmup + args.steps)
+    full_steps = max(1, min(args.steps, 3))
+    (d_ev, pk_ev), ms_f = timed(lambda: multi_ref_align_device(ep, refs, NR, s, s), 1, full_steps)
+    d_ev = d_ev.cpu().numpy()
+    lab = d_ev.argmax(0)
+    r = res.ref.cpu().numpy()
+    same = r == lab
+    full_best = pk_ev.cpu().numpy()[lab, np.arange(P)]
+    same_all = same & np.all(res.params.cpu().numpy() == full_best, axis=1)
+    peak_err = np.abs(res.peak.cpu().numpy().astype(np.float64) - d_ev[lab, np.arange(P)]) / \
+        np.maximum(np.abs(d_ev[lab, np.arange(P)]), 1e-30)
+    return {"workload": w["workload"], "value": P * R / (ms_l / 1000.0), "unit": UNIT,
+            "ms_per_step": ms_l, "steps": args.steps, "warmup": args.warmup,
+            "plain_fp32": {"value": P * R / (ms_f / 1000.0), "ms_per_step": ms_f, "steps": full_steps, "warmup": 1},
+            "ratio_vs_plain_fp32": ms_f / ms_l,
+            "same_best_ref": float(same.mean()), "same_ref_angle_shift_mirror": float(same_all.mean()),
+            "max_rel_peak_err_vs_plain_fp32": float(peak_err.max()),
+            "fallback_rate": float(res.fallback.float().mean().item()),
+            "alignments_run_fraction": res.pairs / (P * R), "k": w["k"], "gap_margin": rep.gap_margin,
+            "calibration": {"recall_top_k": rep.recall, "fallback_rate": rep.fallback_rate,
+                            "max_wrong": w["max_wrong"]},
+            "train": {"particles": n_train, "seconds_incl_labelling": t_train, "loss_first_last":
+                      [rep.loss[0], rep.loss[-1]], "epochs": len(rep.loss)},
+            "gen_seconds": t_gen, "gpu_launches_per_step": launches,
+            "dtype": "f32 network (CUDA cores), f32 search"}
+
+
+def precision_vs_fp64(dev, n=64, R=200):
+    """Peak values of the plain FP32 GPU path against the FP64 oracle on a
+    small stack of the headline workload's shape (same stack on both)."""
+    import torch
+
+    from gpuisac import synth
+    from gpuisac.align import multi_ref_align_device
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    w = WORKLOAD
+    st = synth.make_stack(n, w["img_dim"], R, w["shift_range"], w["snr"], 34.0, synth.SEED_BASE + 1)
+    d, pk = multi_ref_align_device(torch.from_numpy(st.particles).to(dev), torch.from_numpy(st.refs).to(dev),
+                                   w["rings"], 3.0, 3.0)
+    d, pk = d.cpu().numpy(), pk.cpu().numpy()
+    cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, 3.0, 3.0)
+    lay = oracle.reference_layout(cfg)
+    t = time.perf_counter()
+    _, od = oracle.multi_ref_align(cfg, lay, st.particles, st.refs, precision="f64", threads=cpu_threads())
+    t = time.perf_counter() - t
+    od = np.asarray(od, np.float64).reshape(R, n)
+    rel = np.abs(d - od) / np.maximum(np.abs(od), 1e-30)
+    same = d.argmax(0) == od.argmax(0)
+    return {"sample": f"{n} particles x {R} refs, mref workload shape", "max_rel_peak_err": float(rel.max()),
+            "median_rel_peak_err": float(np.median(rel)), "same_best_ref": float(same.mean()),
+            "oracle_seconds": t}
+
+
 def bench_ours(args):
     import torch
 
@@ -290,6 +402,9 @@ def bench_ours(args):
                 "peak_kind": f"bf16 dense, {peak_kind}",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": ccf_avg_ms,
                 "kernel_share": ccf_ms / max(ccf_ms + spec_ms, 1e-9),
+                # the contraction runs in FP32 on CUDA cores: its fraction of the
+                # nominal FP32 FMA rate (152 SMs x 128 lanes x 2 flops x SM clock)
+                "frac_of_fp32_cuda_core_nominal": achieved_tflops / fp32_nominal_tflops(),
                 "spectra_avg_launch_ms": spec_ms / max(spec_launches, 1)}
 
     # ---- end to end through the reference-facing C-ABI ----
@@ -329,13 +444,21 @@ def bench_ours(args):
         cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{n} particles x {R} refs of the same workload, {t:.1f} s (FP32 oracle, OpenMP)"}
 
+    prec = learned_blk = None
+    if rank == 0 and world == 1 and not args.no_learned:
+        del parts_d, d_out, peak_out
+        torch.cuda.empty_cache()
+        prec = precision_vs_fp64(dev)
+        learned_blk = bench_learned(args, dev, L)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantoms, 50k particles/GPU)",
                 "config": dict(WORKLOAD, path="plain FP32 CUDA-core contraction",
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
-                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                "precision_vs_fp64": prec, "learned": learned_blk}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -354,6 +477,9 @@ def main():
     ap.add_argument("--cpu-particles", type=int, default=4000)
     ap.add_argument("--step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-search comparison")
+    ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
+    ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
