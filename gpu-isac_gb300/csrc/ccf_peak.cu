@@ -266,10 +266,12 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8])
                  : "memory");
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-// 16 consecutive columns of the thread's own lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+// 16 consecutive columns of the thread's own lane, left in flight: the
+// registers are valid after tmem_wait_ld16 on the same array, which takes
+// them as operands so that no use is scheduled before the wait
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, float (&v)[16])
 {
-    uint32_t r[16];
+    uint32_t* r = reinterpret_cast<uint32_t*>(v);
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
                  "%13, %14, %15}, [%16];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
@@ -277,10 +279,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
                    "=r"(r[15])
                  : "r"(taddr)
                  : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++)
-        v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld16(float (&v)[16])
+{
+    uint32_t* r = reinterpret_cast<uint32_t*>(v);
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])
+                 :
+                 : "memory");
 }
 } // namespace
 
@@ -329,12 +337,10 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
 {
     constexpr int QT = 4, NSI = 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const unsigned rh0 = (ring_num + 1) / 2; // rings of half 0 (half 1 has ring_num - rh0)
-    const unsigned nrp = 2 * rh0;            // rings per staged shift (one zero ring if odd)
+    const unsigned nrp = 2 * ((ring_num + 1) / 2); // rings per staged shift (one zero ring if odd)
     float2* sbuf = reinterpret_cast<float2*>(smem_raw);                // [NSI][nrp][kSlots]
     float2* zbuf = sbuf + (size_t)NSI * nrp * kSlots;                  // [16][kPairStride]
-    float* xbuf = reinterpret_cast<float*>(zbuf + 16 * kPairStride);   // [2][8][4][kSlots]
-    float2* tw = reinterpret_cast<float2*>(xbuf + 2 * 8 * 4 * kSlots); // [256]
+    float2* tw = zbuf + 16 * kPairStride;                              // [256]
     PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + kRingLen);      // [16]
     uint64_t* bar = reinterpret_cast<uint64_t*>(slots + 16);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
@@ -362,10 +368,8 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
     tmem_fence_before();
     __syncthreads();
     tmem_fence_after();
-    // lane k of the tensor memory holds slot k; columns: [half][ring][ref][u, v]
-    const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(half * kTmemRingsPerHalf * 8);
-    const unsigned r_base = half ? rh0 : 0u;
-    const unsigned rh = half ? ring_num - rh0 : rh0;
+    // lane k of the tensor memory holds slot k; columns: [ring][ref][u, v]
+    const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16);
     const uint32_t row_bytes = ring_num * kSlots * sizeof(float2);
 
     // copies of shift group s0 of particle p of group g (called by thread 0)
@@ -388,21 +392,28 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
     float2* gz = zbuf + g * kPairStride;
 
     while (!failed) {
-        // this item's references -> tensor memory (each thread writes the
-        // columns it will read itself)
-        for (unsigned j = 0; j < (unsigned)kTmemRingsPerHalf; j++) {
-            float v[8];
+        // this item's references -> tensor memory, columns [ring][ref][u, v]
+        // of lane k; the two halves store alternate ring pairs and both read
+        // every ring
+        for (unsigned j = 2 * half; j < nrp; j += 4) {
 #pragma unroll
-            for (int q = 0; q < QT; q++) {
-                float2 uv = make_float2(0.f, 0.f);
-                if (j < rh && q0 + q < grp.n_ref)
-                    uv = __ldg(&grp.ref_sp[((size_t)ref_row(grp, q0 + q) * ring_num + r_base + j) * kSlots + k]);
-                v[2 * q] = uv.x;
-                v[2 * q + 1] = uv.y;
+            for (int jj = 0; jj < 2; jj++) {
+                float v[8];
+#pragma unroll
+                for (int q = 0; q < QT; q++) {
+                    float2 uv = make_float2(0.f, 0.f);
+                    if (j + jj < ring_num && q0 + q < grp.n_ref)
+                        uv = __ldg(&grp.ref_sp[((size_t)ref_row(grp, q0 + q) * ring_num + j + jj) * kSlots + k]);
+                    v[2 * q] = uv.x;
+                    v[2 * q + 1] = uv.y;
+                }
+                tmem_st8(tmem + (j + jj) * 8, v);
             }
-            tmem_st8(tmem + j * 8, v);
         }
         tmem_wait_st();
+        tmem_fence_before();
+        __syncthreads();
+        tmem_fence_after();
         // the item after this one, for the copies issued at its end
         CcfGroup ngrp;
         unsigned nq0 = 0, npb = 0, npe = 0;
@@ -419,44 +430,63 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
                     break;
                 }
                 phase ^= 1u;
-                // ---- contraction: this half's rings, 4 shifts x 4 references ----
-                float acc[QT][NSI][4];
+                // ---- contraction: every ring, this half's 2 shifts x 4 references ----
+                float acc[QT][2][4];
 #pragma unroll
                 for (int q = 0; q < QT; q++)
 #pragma unroll
-                    for (int i = 0; i < NSI; i++)
+                    for (int i = 0; i < 2; i++)
 #pragma unroll
                         for (int c = 0; c < 4; c++)
                             acc[q][i][c] = 0.f;
-                const float2* sb = sbuf + (size_t)r_base * kSlots + k;
-                for (unsigned j = 0; j < rh; j += 2) {
-                    float rv[16]; // rings j, j+1: (u, v) of the 4 references
-                    tmem_ld16(tmem + j * 8, rv);
+                const float2* sb = sbuf + (size_t)(2 * half) * nrp * kSlots + k;
+                // rings j, j+1 from 16 columns; the next pair's load is in
+                // flight while this pair is used
+                auto ring_pair = [&](const float (&rv)[16], unsigned j) {
 #pragma unroll
                     for (int jj = 0; jj < 2; jj++) {
-                        if (j + jj < rh) {
-                            float2 ab[NSI];
-#pragma unroll
-                            for (int i = 0; i < NSI; i++)
-                                ab[i] = sb[((size_t)i * nrp + j + jj) * kSlots];
+                        if (j + jj < ring_num) {
+                            const float2 a0 = sb[(size_t)(j + jj) * kSlots];
+                            const float2 a1 = sb[(size_t)(nrp + j + jj) * kSlots];
 #pragma unroll
                             for (int q = 0; q < QT; q++) {
                                 const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
-#pragma unroll
-                                for (int i = 0; i < NSI; i++) {
-                                    acc[q][i][0] = fmaf(u, ab[i].x, acc[q][i][0]);
-                                    acc[q][i][1] = fmaf(u, ab[i].y, acc[q][i][1]);
-                                    acc[q][i][2] = fmaf(vv, ab[i].y, acc[q][i][2]);
-                                    acc[q][i][3] = fmaf(vv, ab[i].x, acc[q][i][3]);
-                                }
+                                acc[q][0][0] = fmaf(u, a0.x, acc[q][0][0]);
+                                acc[q][0][1] = fmaf(u, a0.y, acc[q][0][1]);
+                                acc[q][0][2] = fmaf(vv, a0.y, acc[q][0][2]);
+                                acc[q][0][3] = fmaf(vv, a0.x, acc[q][0][3]);
+                                acc[q][1][0] = fmaf(u, a1.x, acc[q][1][0]);
+                                acc[q][1][1] = fmaf(u, a1.y, acc[q][1][1]);
+                                acc[q][1][2] = fmaf(vv, a1.y, acc[q][1][2]);
+                                acc[q][1][3] = fmaf(vv, a1.x, acc[q][1][3]);
                             }
                         }
+                    }
+                };
+                {
+                    float ra[16], rb[16];
+                    tmem_ld16_async(tmem, ra);
+                    tmem_wait_ld16(ra);
+                    for (unsigned j = 0; j < nrp; j += 4) {
+                        const bool more_b = j + 2 < nrp;
+                        if (more_b)
+                            tmem_ld16_async(tmem + (j + 2) * 8, rb);
+                        ring_pair(ra, j);
+                        if (!more_b)
+                            break;
+                        tmem_wait_ld16(rb);
+                        const bool more_a = j + 4 < nrp;
+                        if (more_a)
+                            tmem_ld16_async(tmem + (j + 4) * 8, ra);
+                        ring_pair(rb, j + 2);
+                        if (more_a)
+                            tmem_wait_ld16(ra);
                     }
                 }
                 tmem_fence_before();
                 __syncthreads(); // staging area read by everyone; previous FFT phase done with zbuf
                 tmem_fence_after();
-                // next copies overlap the exchange and the FFT phase
+                // next copies overlap the FFT phase
                 if (tid == 0) {
                     if (s0 + NSI < n_shift)
                         issue(grp.sbj_sp, p, s0 + NSI);
@@ -465,33 +495,12 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
                     else if (has_next)
                         issue(ngrp.sbj_sp, npb, 0);
                 }
-                // ---- exchange: half h owns shifts {2h, 2h+1} of the group ----
 #pragma unroll
-                for (int i = 0; i < NSI; i++) {
-                    if ((i >> 1) != half) {
+                for (int ii = 0; ii < 2; ii++)
 #pragma unroll
-                        for (int q = 0; q < QT; q++)
-#pragma unroll
-                            for (int c = 0; c < 4; c++)
-                                xbuf[(((half * 8) + (i & 1) * 4 + q) * 4 + c) * kSlots + k] = acc[q][i][c];
-                    }
-                }
-                __syncthreads();
-#pragma unroll
-                for (int ii = 0; ii < 2; ii++) {
-                    const int i = half * 2 + ii;
-#pragma unroll
-                    for (int q = 0; q < QT; q++) {
-                        float s4[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            // compile-time indices on both sides keep acc in registers
-                            const float mine = half ? acc[q][2 + ii][c] : acc[q][ii][c];
-                            s4[c] = mine + xbuf[((((1 - half) * 8) + ii * 4 + q) * 4 + c) * kSlots + k];
-                        }
-                        write_z(zbuf + (i * QT + q) * kPairStride, k, s4[0], s4[1], s4[2], s4[3]);
-                    }
-                }
+                    for (int q = 0; q < QT; q++)
+                        write_z(zbuf + ((2 * half + ii) * QT + q) * kPairStride, k, acc[q][ii][0], acc[q][ii][1],
+                                acc[q][ii][2], acc[q][ii][3]);
                 __syncthreads();
                 // ---- inverse FFT + peak search, one pair per 16-thread group ----
                 const unsigned s = s0 + g_shift;
@@ -662,7 +671,7 @@ static size_t tma_smem_bytes(unsigned ring_num)
 {
     unsigned nrp = 2 * ((ring_num + 1) / 2);
     return (size_t)4 * nrp * kSlots * sizeof(float2) + 16 * kPairStride * sizeof(float2) +
-           2 * 8 * 4 * kSlots * sizeof(float) + kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16;
+           kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16;
 }
 
 size_t ccf_peak_smem_bytes(unsigned ring_num)

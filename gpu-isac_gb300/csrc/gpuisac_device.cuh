@@ -152,8 +152,24 @@ __device__ __forceinline__ TexPlacement tex_place(const StackDesc& s, unsigned i
 __device__ __forceinline__ const float* tex_row(const StackDesc& s, const TexPlacement& t, long row)
 {
     row = row < 0 ? 0 : (row > t.rows - 1 ? t.rows - 1 : row);
-    unsigned slot = (unsigned)(row / s.dim);
-    unsigned yy = (unsigned)(row - (long)slot * s.dim);
+    // a sample's rows lie in its own image or a neighbour: resolve the slot
+    // without a 64-bit division (the general case keeps it)
+    const int dim = (int)s.dim;
+    const long rel = row - (long)t.local * dim;
+    unsigned slot, yy;
+    if (rel >= 0 && rel < dim) {
+        slot = t.local;
+        yy = (unsigned)rel;
+    } else if (rel < 0 && rel >= -dim) {
+        slot = t.local - 1;
+        yy = (unsigned)(rel + dim);
+    } else if (rel >= dim && rel < 2 * dim) {
+        slot = t.local + 1;
+        yy = (unsigned)(rel - dim);
+    } else {
+        slot = (unsigned)(row / s.dim);
+        yy = (unsigned)(row - (long)slot * s.dim);
+    }
     unsigned g = t.tex_first + slot;
     if (g >= t.batch_end)
         g -= s.batch; // slot not refilled by a short final batch

@@ -15,8 +15,8 @@ constexpr unsigned kMaxShifts = 4096;   // shift grid entries supported
 
 inline size_t polar_spectra_smem_bytes(unsigned ring_num)
 {
-    return (size_t)ring_num * kRingLen * sizeof(float) + 16 * kPairStride * sizeof(float2) +
-           kRingLen * sizeof(float2) + 24 * sizeof(double);
+    return (size_t)((ring_num + 1) / 2) * kPairStride * sizeof(float2) + kRingLen * sizeof(float2) +
+           24 * sizeof(double);
 }
 
 // rings are padded to a multiple of this in the reference tile in shared memory

@@ -20,16 +20,21 @@ namespace gpuisac {
 
 std::atomic<unsigned long long> g_kernel_launches{0};
 
-__global__ void __launch_bounds__(256)
+// smem offset (floats) of ring r's samples
+__device__ __forceinline__ unsigned polar_index(unsigned r) { return (r >> 1) * 2 * kPairStride + (r & 1) * kRingLen; }
+
+__global__ void __launch_bounds__(256, 4)
 polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
                      unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
                      const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
                      float2* __restrict__ out, const unsigned* __restrict__ img_list)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* polar = reinterpret_cast<float*>(smem_raw);                        // [ring_num][256]
-    float2* ws = reinterpret_cast<float2*>(polar + ring_num * kRingLen);      // 16 x kPairStride
-    float2* tw = ws + 16 * kPairStride;                                       // 256
+    // ring pair p's samples at polar[p * 2 * kPairStride + (r & 1) * 256 + angle];
+    // once a pair is in registers its region is the FFT workspace
+    float* polar = reinterpret_cast<float*>(smem_raw);
+    const unsigned n_pairs = (ring_num + 1) / 2;
+    float2* tw = reinterpret_cast<float2*>(polar + n_pairs * 2 * kPairStride);  // 256
     double* red = reinterpret_cast<double*>(tw + kRingLen);                   // 2 x 8 warps + 2
 
     const unsigned row = blockIdx.x;
@@ -55,12 +60,13 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
     // thread tid samples angle tid of every ring; FP32 ring-weighted partial
     // sums feed the FP64 image mean / deviation
     float s1 = 0.f, s2 = 0.f;
+#pragma unroll 4
     for (unsigned r = 0; r < ring_num; r++) {
         float2 o = __ldg(&tmpl[r * kRingLen + tid]);
         float x = cnt_x + o.x;
         float y = (yoff + cnt_y) + o.y;
         float v = tex_sample(st, place, x, y);
-        polar[r * kRingLen + tid] = v;
+        polar[polar_index(r) + tid] = v;
         float w = (float)(r + 1);
         s1 += w * v;
         s2 += w * v * v;
@@ -97,19 +103,20 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
     const int g = tid >> 4;          // FFT group 0..15
     const int l = tid & 15;
     const unsigned gmask = 0xffffu << (tid & 16);
-    float2* gws = ws + g * kPairStride;
-    const unsigned n_pairs = (ring_num + 1) / 2;
     float2* out_row = out + (size_t)row * ring_num * kSlots;
     for (unsigned pr = g; pr < n_pairs; pr += 16) {
         const unsigned ra = 2 * pr, rb = 2 * pr + 1;
         const bool has_b = rb < ring_num;
+        const float* pa = polar + pr * 2 * kPairStride;
+        float2* gws = reinterpret_cast<float2*>(polar) + pr * kPairStride;
         float2 x[16];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
-            float va = (polar[ra * kRingLen + l + 16 * m] - avg_f) * inv_f;
-            float vb = has_b ? (polar[rb * kRingLen + l + 16 * m] - avg_f) * inv_f : 0.f;
+            float va = (pa[l + 16 * m] - avg_f) * inv_f;
+            float vb = has_b ? (pa[kRingLen + l + 16 * m] - avg_f) * inv_f : 0.f;
             x[m] = make_float2(va, vb);
         }
+        __syncwarp(gmask); // the pair's samples are read before its region turns workspace
         fft256_group<-1>(x, gws, tw, l, gmask);
         // natural-order spectrum Z[l + 16 k2] to the workspace
 #pragma unroll
