@@ -152,14 +152,45 @@ __device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, un
     }
 }
 
+// named barrier `id` over n threads (id 0 with n = blockDim is __syncthreads)
+__device__ __forceinline__ void nbar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void nbar_arrive(int id, int n)
+{
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// barrier `id` over n threads that returns whether p held on every one of them
+__device__ __forceinline__ bool nbar_and(int id, int n, bool p)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred pi, po;\n\t"
+                 "setp.ne.u32 pi, %1, 0;\n\t"
+                 "bar.red.and.pred po, %2, %3, pi;\n\t"
+                 "selp.u32 %0, 1, 0, po;\n\t}"
+                 : "=r"(r)
+                 : "r"((uint32_t)p), "r"(id), "r"(n)
+                 : "memory");
+    return r != 0;
+}
+// the barrier of the 256 threads that run the FFT / peak phase
+template <int BAR>
+__device__ __forceinline__ void phase_sync()
+{
+    if (BAR == 0)
+        __syncthreads();
+    else
+        nbar_sync(BAR, 256);
+}
+
 // merge the nsi shift slots of each of the qt references and write the
-// outputs of particle p (all threads call; threads < qt write)
+// outputs of particle p (the 256 threads of the FFT phase call, synchronised
+// by barrier BAR; threads < qt write)
+template <int BAR = 0>
 __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st, int tid, int g, int l, int qt,
                                             int nsi, unsigned q0, unsigned n_ref, unsigned n_shift, unsigned pg,
                                             unsigned p_total, const float2* shifts_f, const float2* base,
                                             float* d_out, float4* peak_out)
 {
-    __syncthreads();
+    phase_sync<BAR>();
     if (l == 0) {
         slots[g].v = st.bv;
         slots[g].h = st.bh;
@@ -167,7 +198,7 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
     }
     if (l < 7)
         slots[g].nb[l] = st.nb;
-    __syncthreads();
+    phase_sync<BAR>();
     if (tid < qt && q0 + tid < n_ref) {
         int best = tid;
         for (int i = 1; i < nsi; i++) {
@@ -186,7 +217,7 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
         d_out[o] = ps.v;
         peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
     }
-    __syncthreads();
+    phase_sync<BAR>();
 }
 
 // ---- mbarrier + bulk async copy (inline PTX) ----
@@ -534,6 +565,286 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
 }
 
 // ============================================================================
+// warp-specialised tensor-memory kernel: 512 threads.  Threads 0..255 stage
+// the subject spectra and run the contraction (references in tensor memory,
+// as above); threads 256..511 run the inverse FFTs and the peak search of the
+// previous shift group at the same time.  The two sides hand over the 16
+// pair spectra through two shared-memory buffers guarded by named barriers
+// (FULL: contraction -> FFT, EMPTY: FFT -> contraction).
+constexpr int kWsBarC = 1;     // contraction side only (256 threads)
+constexpr int kWsBarFull = 2;  // + buffer: 2, 3
+constexpr int kWsBarEmpty = 4; // + buffer: 4, 5
+constexpr int kWsBarF = 6;     // FFT side only (256 threads)
+
+__global__ void __launch_bounds__(512, 1)
+ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift,
+                   const float2* __restrict__ shifts_f, unsigned* __restrict__ err)
+{
+    constexpr int QT = 4, NSI = 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned nrp = 2 * ((ring_num + 1) / 2); // rings per staged shift (one zero ring if odd)
+    float2* sbuf = reinterpret_cast<float2*>(smem_raw);                // [NSI][nrp][kSlots]
+    float2* zbuf = sbuf + (size_t)NSI * nrp * kSlots;                  // [2][16][kPairStride]
+    float2* tw = zbuf + 2 * 16 * kPairStride;                          // [256]
+    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + kRingLen);      // [16]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(slots + 16);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const bool contraction_side = tid < 256;
+
+    unsigned item = blockIdx.x;
+    CcfGroup grp;
+    unsigned q0, pb, pe;
+    if (!decode_item(w, item, QT, grp, q0, pb, pe))
+        return;
+
+    if (tid < kRingLen)
+        tw[tid] = twiddle[tid];
+    for (unsigned i = tid; i < (unsigned)NSI * nrp * kSlots; i += 512)
+        sbuf[i] = make_float2(0.f, 0.f); // the padding ring stays zero
+    if (warp == 0)
+        tmem_alloc(tmem_slot, kTmemCols);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+        *abort_flag = 0;
+    }
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+
+    bool failed = false;
+    uint32_t phase = 0;
+    if (contraction_side) {
+        // ================= contraction side =================
+        const int k = tid & (kSlots - 1);
+        const int half = tid >> 7;
+        // lane k of the tensor memory holds slot k; columns: [ring][ref][u, v]
+        const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16);
+        const uint32_t row_bytes = ring_num * kSlots * sizeof(float2);
+        auto issue = [&](const float2* sp, unsigned p, unsigned s0) {
+            unsigned nv = min((unsigned)NSI, n_shift - s0);
+            fence_proxy_async();
+            mbar_expect_tx(bar, nv * row_bytes);
+            for (unsigned i = 0; i < nv; i++)
+                bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sp + ((size_t)p * n_shift + s0 + i) * ring_num * kSlots,
+                         row_bytes, bar);
+        };
+        bool pending = false; // thread 0: copies in flight
+        if (tid == 0) {
+            issue(grp.sbj_sp, pb, 0);
+            pending = true;
+        }
+        unsigned it = 0;
+        while (!failed) {
+            // this item's references -> tensor memory (both halves read every ring)
+            for (unsigned j = 2 * half; j < nrp; j += 4) {
+#pragma unroll
+                for (int jj = 0; jj < 2; jj++) {
+                    float v[8];
+#pragma unroll
+                    for (int q = 0; q < QT; q++) {
+                        float2 uv = make_float2(0.f, 0.f);
+                        if (j + jj < ring_num && q0 + q < grp.n_ref)
+                            uv = __ldg(&grp.ref_sp[((size_t)ref_row(grp, q0 + q) * ring_num + j + jj) * kSlots + k]);
+                        v[2 * q] = uv.x;
+                        v[2 * q + 1] = uv.y;
+                    }
+                    tmem_st8(tmem + (j + jj) * 8, v);
+                }
+            }
+            tmem_wait_st();
+            tmem_fence_before();
+            nbar_sync(kWsBarC, 256);
+            tmem_fence_after();
+            CcfGroup ngrp;
+            unsigned nq0 = 0, npb = 0, npe = 0;
+            const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
+
+            for (unsigned p = pb; p < pe && !failed; p++) {
+                for (unsigned s0 = 0; s0 < n_shift; s0 += NSI, it++) {
+                    const unsigned b = it & 1u;
+                    // ---- wait for this group's spectra (bounded) ----
+                    const bool ok = mbar_wait(bar, phase);
+                    if (ok && tid == 0)
+                        pending = false;
+                    if (!nbar_and(kWsBarC, 256, ok)) {
+                        // hand the FFT side an empty buffer marked abort
+                        failed = true;
+                        nbar_sync(kWsBarEmpty + b, 512);
+                        if (tid == 0)
+                            *abort_flag = 1;
+                        __threadfence_block();
+                        nbar_arrive(kWsBarFull + b, 512);
+                        break;
+                    }
+                    phase ^= 1u;
+                    float acc[QT][2][4];
+#pragma unroll
+                    for (int q = 0; q < QT; q++)
+#pragma unroll
+                        for (int i = 0; i < 2; i++)
+#pragma unroll
+                            for (int c = 0; c < 4; c++)
+                                acc[q][i][c] = 0.f;
+                    const float2* sb = sbuf + (size_t)(2 * half) * nrp * kSlots + k;
+                    auto ring_pair = [&](const float (&rv)[16], unsigned j) {
+                        float2 pa0[2], pa1[2];
+#pragma unroll
+                        for (int jj = 0; jj < 2; jj++) {
+                            pa0[jj] = sb[(size_t)(j + jj) * kSlots];
+                            pa1[jj] = sb[(size_t)(nrp + j + jj) * kSlots];
+                        }
+#pragma unroll
+                        for (int jj = 0; jj < 2; jj++) {
+                            if (j + jj < ring_num) {
+                                const float2 a0 = pa0[jj];
+                                const float2 a1 = pa1[jj];
+#pragma unroll
+                                for (int q = 0; q < QT; q++) {
+                                    const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
+                                    acc[q][0][0] = fmaf(u, a0.x, acc[q][0][0]);
+                                    acc[q][0][1] = fmaf(u, a0.y, acc[q][0][1]);
+                                    acc[q][0][2] = fmaf(vv, a0.y, acc[q][0][2]);
+                                    acc[q][0][3] = fmaf(vv, a0.x, acc[q][0][3]);
+                                    acc[q][1][0] = fmaf(u, a1.x, acc[q][1][0]);
+                                    acc[q][1][1] = fmaf(u, a1.y, acc[q][1][1]);
+                                    acc[q][1][2] = fmaf(vv, a1.y, acc[q][1][2]);
+                                    acc[q][1][3] = fmaf(vv, a1.x, acc[q][1][3]);
+                                }
+                            }
+                        }
+                    };
+                    {
+                        float ra[16], rb[16];
+                        tmem_ld16_async(tmem, ra);
+                        tmem_wait_ld16(ra);
+                        for (unsigned j = 0; j < nrp; j += 4) {
+                            const bool more_b = j + 2 < nrp;
+                            if (more_b)
+                                tmem_ld16_async(tmem + (j + 2) * 8, rb);
+                            ring_pair(ra, j);
+                            if (!more_b)
+                                break;
+                            tmem_wait_ld16(rb);
+                            const bool more_a = j + 4 < nrp;
+                            if (more_a)
+                                tmem_ld16_async(tmem + (j + 4) * 8, ra);
+                            ring_pair(rb, j + 2);
+                            if (more_a)
+                                tmem_wait_ld16(ra);
+                        }
+                    }
+                    tmem_fence_before();
+                    nbar_sync(kWsBarC, 256); // the staging area is consumed
+                    tmem_fence_after();
+                    if (tid == 0) {
+                        const float2* n_sp = nullptr;
+                        unsigned n_p = 0, n_s0 = 0;
+                        if (s0 + NSI < n_shift) {
+                            n_sp = grp.sbj_sp;
+                            n_p = p;
+                            n_s0 = s0 + NSI;
+                        } else if (p + 1 < pe) {
+                            n_sp = grp.sbj_sp;
+                            n_p = p + 1;
+                        } else if (has_next) {
+                            n_sp = ngrp.sbj_sp;
+                            n_p = npb;
+                        }
+                        if (n_sp) {
+                            issue(n_sp, n_p, n_s0);
+                            pending = true;
+                        }
+                    }
+                    // ---- hand the pair spectra to the FFT side ----
+                    float2* zb = zbuf + (size_t)b * 16 * kPairStride;
+                    nbar_sync(kWsBarEmpty + b, 512);
+#pragma unroll
+                    for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+                        for (int q = 0; q < QT; q++)
+                            write_z(zb + ((2 * half + ii) * QT + q) * kPairStride, k, acc[q][ii][0], acc[q][ii][1],
+                                    acc[q][ii][2], acc[q][ii][3]);
+                    __threadfence_block();
+                    nbar_arrive(kWsBarFull + b, 512);
+                }
+            }
+            if (failed || !has_next)
+                break;
+            item += gridDim.x;
+            grp = ngrp;
+            q0 = nq0;
+            pb = npb;
+            pe = npe;
+            // the next item's references overwrite tensor memory: every
+            // contraction of this item is done
+            tmem_fence_before();
+            nbar_sync(kWsBarC, 256);
+            tmem_fence_after();
+        }
+        if (failed && tid == 0) {
+            atomicExch(err, 1u);
+            if (pending)
+                mbar_wait(bar, phase); // let copies in flight land before leaving (bounded)
+        }
+    } else {
+        // ================= FFT / peak side =================
+        const int ftid = tid - 256;
+        const int g = ftid >> 4, l = ftid & 15;
+        const unsigned gmask = 0xffffu << (ftid & 16);
+        const int g_shift = g / QT;
+        // both buffers start empty
+        nbar_arrive(kWsBarEmpty + 0, 512);
+        nbar_arrive(kWsBarEmpty + 1, 512);
+        unsigned it = 0;
+        while (!failed) {
+            CcfGroup ngrp;
+            unsigned nq0 = 0, npb = 0, npe = 0;
+            const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
+            for (unsigned p = pb; p < pe && !failed; p++) {
+                PeakState st;
+                st.reset();
+                for (unsigned s0 = 0; s0 < n_shift; s0 += NSI, it++) {
+                    const unsigned b = it & 1u;
+                    nbar_sync(kWsBarFull + b, 512);
+                    if (*abort_flag) {
+                        failed = true;
+                        break;
+                    }
+                    float2* gz = zbuf + (size_t)b * 16 * kPairStride + g * kPairStride;
+                    const unsigned s = s0 + g_shift;
+                    if (s < n_shift)
+                        fft_peak(gz, tw, l, gmask, s, n_shift, st);
+                    __threadfence_block();
+                    nbar_arrive(kWsBarEmpty + b, 512);
+                }
+                if (failed)
+                    break;
+                merge_write<kWsBarF>(slots, st, ftid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p,
+                                     grp.p_total, shifts_f, grp.base, grp.d_out, grp.peak_out);
+            }
+            if (failed || !has_next)
+                break;
+            item += gridDim.x;
+            grp = ngrp;
+            q0 = nq0;
+            pb = npb;
+            pe = npe;
+        }
+    }
+    // release the tensor memory (all tcgen05 accesses of the CTA are done)
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 0)
+        tmem_dealloc(*tmem_slot, kTmemCols);
+}
+
+// ============================================================================
 // general kernel: references in shared memory, subject spectra in registers;
 // persistent over work items
 template <int QT>
@@ -674,10 +985,17 @@ static size_t tma_smem_bytes(unsigned ring_num)
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16;
 }
 
+static size_t ws_smem_bytes(unsigned ring_num)
+{
+    unsigned nrp = 2 * ((ring_num + 1) / 2);
+    return (size_t)4 * nrp * kSlots * sizeof(float2) + 2 * 16 * kPairStride * sizeof(float2) +
+           kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16;
+}
+
+// shared memory of the general kernel (references in shared memory) at any
+// ring count
 size_t ccf_peak_smem_bytes(unsigned ring_num)
 {
-    if (ring_num <= kTmaMaxRings)
-        return tma_smem_bytes(ring_num);
     unsigned qt = ccf_refs_per_cta(ring_num);
     return (size_t)qt * ring_pad(ring_num) * kSlots * sizeof(float2) + 16 * kPairStride * sizeof(float2) +
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot);
@@ -685,17 +1003,24 @@ size_t ccf_peak_smem_bytes(unsigned ring_num)
 
 unsigned ccf_refs_per_item(unsigned ring_num, int variant)
 {
-    if (variant == kCcfTmem && ring_num <= kTmaMaxRings)
+    if ((variant == kCcfTmem || variant == kCcfWs) && ring_num <= kTmaMaxRings)
         return 4;
     return ccf_refs_per_cta(ring_num);
 }
 
 int ccf_variant(unsigned ring_num, bool aligned)
 {
-    // GPUISAC_CCF_KERNEL=general selects the general kernel for every ring count
+    // GPUISAC_CCF_KERNEL=general selects the general kernel for every ring
+    // count, =tmem the single-phase tensor-memory kernel; the default up to
+    // kTmaMaxRings rings is the warp-specialised one
     const char* sel = getenv("GPUISAC_CCF_KERNEL");
-    const bool force_general = sel && strcmp(sel, "general") == 0;
-    return (ring_num <= kTmaMaxRings && aligned && !force_general) ? kCcfTmem : kCcfGeneral;
+    if (sel && strcmp(sel, "general") == 0)
+        return kCcfGeneral;
+    if (ring_num > kTmaMaxRings || !aligned)
+        return kCcfGeneral;
+    if (sel && strcmp(sel, "tmem") == 0)
+        return kCcfTmem;
+    return kCcfWs;
 }
 
 template <typename K>
@@ -722,7 +1047,17 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* tw
     if (w.n_items == 0)
         return cudaSuccess;
     const unsigned grid = persistent_grid(w.n_items, 1);
-    if (variant == kCcfTmem) {
+    if (variant == kCcfWs) {
+        static int configured = 0;
+        if (!configured) {
+            cudaError_t e = set_max_smem(ccf_peak_ws_kernel);
+            if (e != cudaSuccess)
+                return e;
+            configured = 1;
+        }
+        ccf_peak_ws_kernel<<<grid, 512, ws_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift, shifts_f,
+                                                                          err);
+    } else if (variant == kCcfTmem) {
         static int configured = 0;
         if (!configured) {
             cudaError_t e = set_max_smem(ccf_peak_tmem_kernel);

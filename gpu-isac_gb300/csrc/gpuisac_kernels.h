@@ -71,7 +71,7 @@ struct CcfWork {
     unsigned ppc; // particles per work item
 };
 
-enum { kCcfGeneral = 0, kCcfTmem = 1 };
+enum { kCcfGeneral = 0, kCcfTmem = 1, kCcfWs = 2 };
 constexpr unsigned kCcfParticlesPerItem = 8;
 
 // kernel variant for a ring count (aligned: spectra rows 16-byte aligned)

@@ -127,3 +127,21 @@ def test_repeated_calls_are_identical(gpulib, cuda, small_case):
     a = multi_ref_align(st.particles[:40], st.refs, 29, 2.0, 2.0)
     b = multi_ref_align(st.particles[:40], st.refs, 29, 2.0, 2.0)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("NR", [29, 35, 36, 3])
+def test_ccf_kernel_variants_agree(gpulib, cuda, oracle_mod, NR, monkeypatch):
+    """The warp-specialised kernel (default), the single-phase tensor-memory
+    kernel and the general kernel: the first two run the same arithmetic in
+    the same order (bit-identical), the general one sums the rings in another
+    order (tolerance)."""
+    from gpuisac import multi_ref_align
+    st = synth.make_stack(70, 76, 9, 3, 0.05, 34.0, 41)
+    runs = {}
+    for sel in ("", "tmem", "general"):
+        monkeypatch.setenv("GPUISAC_CCF_KERNEL", sel)
+        runs[sel] = multi_ref_align(st.particles, st.refs, NR, 3.0, 3.0)
+    monkeypatch.delenv("GPUISAC_CCF_KERNEL")
+    assert np.array_equal(runs[""][0], runs["tmem"][0]) and np.array_equal(runs[""][1], runs["tmem"][1])
+    d0, dg = runs[""][1].astype(np.float64), runs["general"][1].astype(np.float64)
+    assert (np.abs(d0 - dg) / np.maximum(np.abs(dg), 1e-30)).max() <= PEAK_RTOL
