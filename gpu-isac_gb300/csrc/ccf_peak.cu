@@ -576,11 +576,18 @@ constexpr int kWsBarFull = 2;  // + buffer: 2, 3
 constexpr int kWsBarEmpty = 4; // + buffer: 4, 5
 constexpr int kWsBarF = 6;     // FFT side only (256 threads)
 
-__global__ void __launch_bounds__(512, 1)
+// CW contraction warps (4: one thread per slot k with all 4 shifts; 8: two
+// threads per slot k with 2 shifts each) + 8 FFT warps
+template <int CW>
+__global__ void __launch_bounds__(32 * CW + 256, 1)
 ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift,
                    const float2* __restrict__ shifts_f, unsigned* __restrict__ err)
 {
     constexpr int QT = 4, NSI = 4;
+    constexpr int NC = 32 * CW;        // contraction threads
+    constexpr int NT = NC + 256;       // all threads
+    constexpr int SPT = NSI * 128 / NC; // shifts per contraction thread
+    static_assert(CW == 4 || CW == 8, "4 or 8 contraction warps");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned nrp = 2 * ((ring_num + 1) / 2); // rings per staged shift (one zero ring if odd)
     float2* sbuf = reinterpret_cast<float2*>(smem_raw);                // [NSI][nrp][kSlots]
@@ -593,7 +600,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
-    const bool contraction_side = tid < 256;
+    const bool contraction_side = tid < NC;
 
     unsigned item = blockIdx.x;
     CcfGroup grp;
@@ -603,7 +610,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
 
     if (tid < kRingLen)
         tw[tid] = twiddle[tid];
-    for (unsigned i = tid; i < (unsigned)NSI * nrp * kSlots; i += 512)
+    for (unsigned i = tid; i < (unsigned)NSI * nrp * kSlots; i += NT)
         sbuf[i] = make_float2(0.f, 0.f); // the padding ring stays zero
     if (warp == 0)
         tmem_alloc(tmem_slot, kTmemCols);
@@ -621,7 +628,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
     if (contraction_side) {
         // ================= contraction side =================
         const int k = tid & (kSlots - 1);
-        const int half = tid >> 7;
+        const int half = tid >> 7; // which SPT shifts of the group (0 when CW = 4)
         // lane k of the tensor memory holds slot k; columns: [ring][ref][u, v]
         const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16);
         const uint32_t row_bytes = ring_num * kSlots * sizeof(float2);
@@ -641,7 +648,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
         unsigned it = 0;
         while (!failed) {
             // this item's references -> tensor memory (both halves read every ring)
-            for (unsigned j = 2 * half; j < nrp; j += 4) {
+            for (unsigned j = 2 * half; j < nrp; j += 2 * (NC / 128)) {
 #pragma unroll
                 for (int jj = 0; jj < 2; jj++) {
                     float v[8];
@@ -658,7 +665,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             }
             tmem_wait_st();
             tmem_fence_before();
-            nbar_sync(kWsBarC, 256);
+            nbar_sync(kWsBarC, NC);
             tmem_fence_after();
             CcfGroup ngrp;
             unsigned nq0 = 0, npb = 0, npe = 0;
@@ -671,49 +678,47 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     const bool ok = mbar_wait(bar, phase);
                     if (ok && tid == 0)
                         pending = false;
-                    if (!nbar_and(kWsBarC, 256, ok)) {
+                    if (!nbar_and(kWsBarC, NC, ok)) {
                         // hand the FFT side an empty buffer marked abort
                         failed = true;
-                        nbar_sync(kWsBarEmpty + b, 512);
+                        nbar_sync(kWsBarEmpty + b, NT);
                         if (tid == 0)
                             *abort_flag = 1;
                         __threadfence_block();
-                        nbar_arrive(kWsBarFull + b, 512);
+                        nbar_arrive(kWsBarFull + b, NT);
                         break;
                     }
                     phase ^= 1u;
-                    float acc[QT][2][4];
+                    float acc[QT][SPT][4];
 #pragma unroll
                     for (int q = 0; q < QT; q++)
 #pragma unroll
-                        for (int i = 0; i < 2; i++)
+                        for (int i = 0; i < SPT; i++)
 #pragma unroll
                             for (int c = 0; c < 4; c++)
                                 acc[q][i][c] = 0.f;
-                    const float2* sb = sbuf + (size_t)(2 * half) * nrp * kSlots + k;
+                    const float2* sb = sbuf + (size_t)(SPT * half) * nrp * kSlots + k;
                     auto ring_pair = [&](const float (&rv)[16], unsigned j) {
-                        float2 pa0[2], pa1[2];
+                        float2 pa[2][SPT];
 #pragma unroll
-                        for (int jj = 0; jj < 2; jj++) {
-                            pa0[jj] = sb[(size_t)(j + jj) * kSlots];
-                            pa1[jj] = sb[(size_t)(nrp + j + jj) * kSlots];
-                        }
+                        for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+                            for (int i = 0; i < SPT; i++)
+                                pa[jj][i] = sb[(size_t)(i * nrp + j + jj) * kSlots];
 #pragma unroll
                         for (int jj = 0; jj < 2; jj++) {
                             if (j + jj < ring_num) {
-                                const float2 a0 = pa0[jj];
-                                const float2 a1 = pa1[jj];
 #pragma unroll
                                 for (int q = 0; q < QT; q++) {
                                     const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
-                                    acc[q][0][0] = fmaf(u, a0.x, acc[q][0][0]);
-                                    acc[q][0][1] = fmaf(u, a0.y, acc[q][0][1]);
-                                    acc[q][0][2] = fmaf(vv, a0.y, acc[q][0][2]);
-                                    acc[q][0][3] = fmaf(vv, a0.x, acc[q][0][3]);
-                                    acc[q][1][0] = fmaf(u, a1.x, acc[q][1][0]);
-                                    acc[q][1][1] = fmaf(u, a1.y, acc[q][1][1]);
-                                    acc[q][1][2] = fmaf(vv, a1.y, acc[q][1][2]);
-                                    acc[q][1][3] = fmaf(vv, a1.x, acc[q][1][3]);
+#pragma unroll
+                                    for (int i = 0; i < SPT; i++) {
+                                        const float2 a = pa[jj][i];
+                                        acc[q][i][0] = fmaf(u, a.x, acc[q][i][0]);
+                                        acc[q][i][1] = fmaf(u, a.y, acc[q][i][1]);
+                                        acc[q][i][2] = fmaf(vv, a.y, acc[q][i][2]);
+                                        acc[q][i][3] = fmaf(vv, a.x, acc[q][i][3]);
+                                    }
                                 }
                             }
                         }
@@ -739,7 +744,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                         }
                     }
                     tmem_fence_before();
-                    nbar_sync(kWsBarC, 256); // the staging area is consumed
+                    nbar_sync(kWsBarC, NC); // the staging area is consumed
                     tmem_fence_after();
                     if (tid == 0) {
                         const float2* n_sp = nullptr;
@@ -762,15 +767,15 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     }
                     // ---- hand the pair spectra to the FFT side ----
                     float2* zb = zbuf + (size_t)b * 16 * kPairStride;
-                    nbar_sync(kWsBarEmpty + b, 512);
+                    nbar_sync(kWsBarEmpty + b, NT);
 #pragma unroll
-                    for (int ii = 0; ii < 2; ii++)
+                    for (int ii = 0; ii < SPT; ii++)
 #pragma unroll
                         for (int q = 0; q < QT; q++)
-                            write_z(zb + ((2 * half + ii) * QT + q) * kPairStride, k, acc[q][ii][0], acc[q][ii][1],
+                            write_z(zb + ((SPT * half + ii) * QT + q) * kPairStride, k, acc[q][ii][0], acc[q][ii][1],
                                     acc[q][ii][2], acc[q][ii][3]);
                     __threadfence_block();
-                    nbar_arrive(kWsBarFull + b, 512);
+                    nbar_arrive(kWsBarFull + b, NT);
                 }
             }
             if (failed || !has_next)
@@ -783,7 +788,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             // the next item's references overwrite tensor memory: every
             // contraction of this item is done
             tmem_fence_before();
-            nbar_sync(kWsBarC, 256);
+            nbar_sync(kWsBarC, NC);
             tmem_fence_after();
         }
         if (failed && tid == 0) {
@@ -793,13 +798,13 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
         }
     } else {
         // ================= FFT / peak side =================
-        const int ftid = tid - 256;
+        const int ftid = tid - NC;
         const int g = ftid >> 4, l = ftid & 15;
         const unsigned gmask = 0xffffu << (ftid & 16);
         const int g_shift = g / QT;
         // both buffers start empty
-        nbar_arrive(kWsBarEmpty + 0, 512);
-        nbar_arrive(kWsBarEmpty + 1, 512);
+        nbar_arrive(kWsBarEmpty + 0, NT);
+        nbar_arrive(kWsBarEmpty + 1, NT);
         unsigned it = 0;
         while (!failed) {
             CcfGroup ngrp;
@@ -810,7 +815,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                 st.reset();
                 for (unsigned s0 = 0; s0 < n_shift; s0 += NSI, it++) {
                     const unsigned b = it & 1u;
-                    nbar_sync(kWsBarFull + b, 512);
+                    nbar_sync(kWsBarFull + b, NT);
                     if (*abort_flag) {
                         failed = true;
                         break;
@@ -820,7 +825,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     if (s < n_shift)
                         fft_peak(gz, tw, l, gmask, s, n_shift, st);
                     __threadfence_block();
-                    nbar_arrive(kWsBarEmpty + b, 512);
+                    nbar_arrive(kWsBarEmpty + b, NT);
                 }
                 if (failed)
                     break;
@@ -1048,15 +1053,28 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* tw
         return cudaSuccess;
     const unsigned grid = persistent_grid(w.n_items, 1);
     if (variant == kCcfWs) {
-        static int configured = 0;
-        if (!configured) {
-            cudaError_t e = set_max_smem(ccf_peak_ws_kernel);
-            if (e != cudaSuccess)
-                return e;
-            configured = 1;
+        const char* cw = getenv("GPUISAC_CCF_WS_WARPS");
+        if (cw && strcmp(cw, "4") == 0) {
+            static int configured = 0;
+            if (!configured) {
+                cudaError_t e = set_max_smem(ccf_peak_ws_kernel<4>);
+                if (e != cudaSuccess)
+                    return e;
+                configured = 1;
+            }
+            ccf_peak_ws_kernel<4><<<grid, 384, ws_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift,
+                                                                                 shifts_f, err);
+        } else {
+            static int configured = 0;
+            if (!configured) {
+                cudaError_t e = set_max_smem(ccf_peak_ws_kernel<8>);
+                if (e != cudaSuccess)
+                    return e;
+                configured = 1;
+            }
+            ccf_peak_ws_kernel<8><<<grid, 512, ws_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift,
+                                                                                 shifts_f, err);
         }
-        ccf_peak_ws_kernel<<<grid, 512, ws_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift, shifts_f,
-                                                                          err);
     } else if (variant == kCcfTmem) {
         static int configured = 0;
         if (!configured) {
