@@ -282,6 +282,71 @@ def bench_learned(args, dev, L):
             "dtype": "f32 network (CUDA cores), f32 search"}
 
 
+GROUPED = dict(workload="groups_400_loguniform_100_5000_x76_10to60ref", n_groups=400, min_size=100, max_size=5000,
+               min_refs=10, max_refs=60, img_dim=76, rings=35, shift_range=3, n_shifts=49)
+
+
+def bench_grouped(args, dev, L, parts_d, refs_d):
+    """400 independent groups in one persistent, graph-captured launch
+    sequence (gpuisac_multi_ref_align_groups_device) against the same groups
+    run one call each; tile shape from the autotuner.  Group sizes are
+    log-uniform in [100, 5000] particles with 10..60 references each, cut
+    from the 50,000-particle / 200-reference stacks already resident (groups
+    may overlap in the pool; each is its own stack)."""
+    import torch
+
+    from gpuisac.align import ccf_tile_name, multi_ref_align_device, multi_ref_align_groups_device
+    g = GROUPED
+    P, R = parts_d.shape[0], refs_d.shape[0]
+    rng = np.random.Generator(np.random.PCG64(20261203 + 2))
+    sizes = np.exp(rng.uniform(np.log(g["min_size"]), np.log(g["max_size"]), g["n_groups"])).astype(int)
+    nrefs = rng.integers(g["min_refs"], g["max_refs"] + 1, g["n_groups"])
+    groups = []
+    for n, r in zip(sizes, nrefs):
+        so = int(rng.integers(0, P - n + 1))
+        ro = int(rng.integers(0, R - r + 1))
+        groups.append((so, int(n), ro, int(r)))
+    alignments = int(sum(n * r for _, n, _, r in groups))
+    NR, s = g["rings"], float(g["shift_range"])
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, warm, steps):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = None
+        for _ in range(steps):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1) / steps
+
+    launches0 = L.gpuisac_launch_count()
+    (dg, pg, offs), ms_g = timed(lambda: multi_ref_align_groups_device(parts_d, refs_d, groups, NR, s, s),
+                                 max(args.warmup, 1), args.steps)
+    launches = (L.gpuisac_launch_count() - launches0) / (max(args.warmup, 1) + args.steps)
+
+    def sequential():
+        return [multi_ref_align_device(parts_d[so:so + n], refs_d[ro:ro + r], NR, s, s) for so, n, ro, r in groups]
+
+    seq, ms_s = timed(sequential, 1, 1)
+    same = 0
+    dg_h, pg_h = dg.cpu().numpy(), pg.cpu().numpy()
+    for (so, n, ro, r), off, (d1, p1) in zip(groups, offs, seq):
+        same += int(np.array_equal(dg_h[off:off + n * r].reshape(r, n), d1.cpu().numpy()) and
+                    np.array_equal(pg_h[off:off + n * r].reshape(r, n, 4), p1.cpu().numpy()))
+    return {"workload": g["workload"], "value": alignments / (ms_g / 1000.0), "unit": UNIT, "ms_per_step": ms_g,
+            "steps": args.steps, "warmup": max(args.warmup, 1), "alignments_per_step": alignments,
+            "particles_per_step": int(sizes.sum()),
+            "sequential_per_group_calls": {"value": alignments / (ms_s / 1000.0), "ms": ms_s},
+            "groups_identical_to_sequential": f"{same}/{len(groups)}",
+            "tile": ccf_tile_name(NR, g["n_shifts"]),
+            "kernel_launches_per_step_incl_graph_nodes": launches,
+            "data": "groups cut from the resident 50k-particle / 200-ref synthetic stacks"}
+
+
 def precision_vs_fp64(dev, n=64, R=200):
     """Peak values of the plain FP32 GPU path against the FP64 oracle on a
     small stack of the headline workload's shape (same stack on both)."""
@@ -348,6 +413,13 @@ def bench_ours(args):
     def barrier():
         if world > 1:
             torch.distributed.barrier()
+
+    # tile shape of the CCF launches: the autotuner times the candidates on a
+    # sample of this workload (setup, untimed)
+    from gpuisac.align import autotune_ccf
+    t0 = time.perf_counter()
+    tune_report = autotune_ccf(parts_d, refs_d, w["rings"], 3.0, 3.0, n_sample=2048, stream=stream)
+    tune = {"seconds": time.perf_counter() - t0, "report": tune_report}
 
     for _ in range(args.warmup):
         step()
@@ -453,9 +525,13 @@ def bench_ours(args):
         cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{n} particles x {R} refs of the same workload, {t:.1f} s (FP32 oracle, OpenMP)"}
 
-    prec = learned_blk = None
+    prec = learned_blk = grouped_blk = None
+    if rank == 0 and world == 1 and not args.no_grouped:
+        del d_out, peak_out
+        torch.cuda.empty_cache()
+        grouped_blk = bench_grouped(args, dev, L, parts_d, refs_d)
     if rank == 0 and world == 1 and not args.no_learned:
-        del parts_d, d_out, peak_out
+        del parts_d
         torch.cuda.empty_cache()
         prec = precision_vs_fp64(dev)
         learned_blk = bench_learned(args, dev, L)
@@ -464,10 +540,10 @@ def bench_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantoms, 50k particles/GPU)",
-                "config": dict(WORKLOAD, path="plain FP32 CUDA-core contraction",
+                "config": dict(WORKLOAD, path="plain FP32 CUDA-core contraction", autotune=tune,
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-                "precision_vs_fp64": prec, "learned": learned_blk}
+                "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -487,6 +563,7 @@ def main():
     ap.add_argument("--step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-search comparison")
+    ap.add_argument("--no-grouped", action="store_true", help="skip the grouped-launch comparison")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])
     args = ap.parse_args()

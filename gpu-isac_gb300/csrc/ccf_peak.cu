@@ -32,6 +32,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <map>
+#include <mutex>
 
 #include "gpuisac_device.cuh"
 #include "gpuisac_kernels.h"
@@ -1013,20 +1016,64 @@ unsigned ccf_refs_per_item(unsigned ring_num, int variant)
     return ccf_refs_per_cta(ring_num);
 }
 
-int ccf_variant(unsigned ring_num, bool aligned)
+namespace {
+std::mutex g_tile_mu;
+std::map<std::pair<unsigned, unsigned>, CcfTile> g_tiles;
+std::atomic<unsigned> g_tile_gen{0};
+thread_local const CcfTile* t_forced = nullptr;
+} // namespace
+
+void ccf_tile_record(unsigned ring_num, unsigned n_shift, const CcfTile& t)
 {
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    g_tiles[{ring_num, n_shift}] = t;
+    g_tile_gen.fetch_add(1);
+}
+
+bool ccf_tile_lookup(unsigned ring_num, unsigned n_shift, CcfTile& t)
+{
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    auto it = g_tiles.find({ring_num, n_shift});
+    if (it == g_tiles.end())
+        return false;
+    t = it->second;
+    return true;
+}
+
+void ccf_tile_force(const CcfTile* t) { t_forced = t; }
+
+unsigned ccf_tile_generation() { return g_tile_gen.load(); }
+
+CcfTile ccf_tile(unsigned ring_num, unsigned n_shift, bool aligned)
+{
+    CcfTile t{kCcfWs, 8, kCcfParticlesPerItem};
+    if (t_forced)
+        t = *t_forced;
+    else
+        ccf_tile_lookup(ring_num, n_shift, t);
     // GPUISAC_CCF_KERNEL=general selects the general kernel for every ring
-    // count, =tmem the single-phase tensor-memory kernel; the default up to
-    // kTmaMaxRings rings is the warp-specialised one
+    // count, =tmem the single-phase tensor-memory kernel, =ws the
+    // warp-specialised one; GPUISAC_CCF_WS_WARPS=4|8 its contraction warps
     const char* sel = getenv("GPUISAC_CCF_KERNEL");
     if (sel && strcmp(sel, "general") == 0)
-        return kCcfGeneral;
+        t.variant = kCcfGeneral;
+    else if (sel && strcmp(sel, "tmem") == 0)
+        t.variant = kCcfTmem;
+    else if (sel && strcmp(sel, "ws") == 0)
+        t.variant = kCcfWs;
+    const char* cw = getenv("GPUISAC_CCF_WS_WARPS");
+    if (cw && (strcmp(cw, "4") == 0 || strcmp(cw, "8") == 0))
+        t.ws_warps = cw[0] - '0';
     if (ring_num > kTmaMaxRings || !aligned)
-        return kCcfGeneral;
-    if (sel && strcmp(sel, "tmem") == 0)
-        return kCcfTmem;
-    return kCcfWs;
+        t.variant = kCcfGeneral;
+    if (t.ws_warps != 4)
+        t.ws_warps = 8;
+    if (t.ppc == 0)
+        t.ppc = kCcfParticlesPerItem;
+    return t;
 }
+
+int ccf_variant(unsigned ring_num, bool aligned, unsigned n_shift) { return ccf_tile(ring_num, n_shift, aligned).variant; }
 
 template <typename K>
 static cudaError_t set_max_smem(K kernel)
@@ -1053,8 +1100,7 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* tw
         return cudaSuccess;
     const unsigned grid = persistent_grid(w.n_items, 1);
     if (variant == kCcfWs) {
-        const char* cw = getenv("GPUISAC_CCF_WS_WARPS");
-        if (cw && strcmp(cw, "4") == 0) {
+        if (ccf_tile(ring_num, n_shift, true).ws_warps == 4) {
             static int configured = 0;
             if (!configured) {
                 cudaError_t e = set_max_smem(ccf_peak_ws_kernel<4>);
@@ -1119,12 +1165,13 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
         return cudaSuccess;
     // bulk copies need 16-byte aligned sources (every row is a multiple of 1 KiB)
     const bool aligned = ((uintptr_t)sbj_sp & 15) == 0 && err != nullptr;
-    const int variant = ccf_variant(ring_num, aligned);
+    const CcfTile tile = ccf_tile(ring_num, n_shift, aligned);
+    const int variant = tile.variant;
     const unsigned qt = ccf_refs_per_item(ring_num, variant);
     CcfWork w{};
     w.groups = nullptr;
     w.n_groups = 1;
-    w.ppc = kCcfParticlesPerItem;
+    w.ppc = tile.ppc;
     CcfGroup& g = w.one;
     g.sbj_sp = sbj_sp;
     g.ref_sp = ref_sp;

@@ -74,8 +74,25 @@ struct CcfWork {
 enum { kCcfGeneral = 0, kCcfTmem = 1, kCcfWs = 2 };
 constexpr unsigned kCcfParticlesPerItem = 8;
 
+// Tile shape of the CCF launch: kernel variant, contraction warps of the
+// warp-specialised kernel, particles per work item.  Chosen per (ring count,
+// shift count): GPUISAC_CCF_KERNEL / GPUISAC_CCF_WS_WARPS override, then a
+// candidate forced on this thread by the autotuner while it times it, then
+// the autotuner's recorded choice, then the default (ws, 8, 8).
+struct CcfTile {
+    int variant;
+    int ws_warps;
+    unsigned ppc;
+};
+CcfTile ccf_tile(unsigned ring_num, unsigned n_shift, bool aligned);
+void ccf_tile_record(unsigned ring_num, unsigned n_shift, const CcfTile& t);
+void ccf_tile_force(const CcfTile* t); // this thread only; nullptr clears
+bool ccf_tile_lookup(unsigned ring_num, unsigned n_shift, CcfTile& t);
+// bumped whenever a choice is recorded (cached launch graphs compare it)
+unsigned ccf_tile_generation();
+
 // kernel variant for a ring count (aligned: spectra rows 16-byte aligned)
-int ccf_variant(unsigned ring_num, bool aligned);
+int ccf_variant(unsigned ring_num, bool aligned, unsigned n_shift = 0);
 // references per work item of that variant
 unsigned ccf_refs_per_item(unsigned ring_num, int variant);
 

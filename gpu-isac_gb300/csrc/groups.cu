@@ -148,6 +148,8 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     append(key, ptrs, sizeof(ptrs));
     append(key, &dev, sizeof(dev));
     append(key, &st, sizeof(st));
+    const CcfTile key_tile = ccf_tile(geo.NR, geo.S, true); // another tile shape records a new graph
+    append(key, &key_tile, sizeof(key_tile));
     if (S.plan.exec && S.plan.key == key) {
         G_CK(cudaMemsetAsync(S.err.p, 0, sizeof(unsigned), st));
         G_CK(cudaGraphLaunch(S.plan.exec, st));
@@ -162,9 +164,10 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     const unsigned NR = geo.NR, Sn = geo.S, D = geo.D;
     const size_t row_elems = (size_t)NR * kSlots;
     const unsigned tex = texture_images(dev, D);
-    const int variant = ccf_variant(NR, true);
+    const CcfTile tile = ccf_tile(NR, Sn, true);
+    const int variant = tile.variant;
     const unsigned qt = ccf_refs_per_item(NR, variant);
-    const unsigned ppc = kCcfParticlesPerItem;
+    const unsigned ppc = tile.ppc;
 
     size_t free_b = 0, total_b = 0;
     G_CK(cudaMemGetInfo(&free_b, &total_b));

@@ -93,7 +93,7 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
     const unsigned NR = geo.NR, Sn = geo.S, D = geo.D;
     const size_t row_elems = (size_t)NR * kSlots;
     const unsigned tex = texture_images(dev, D);
-    const int variant = ccf_variant(NR, true);
+    const int variant = ccf_variant(NR, true, Sn);
     const unsigned qt = ccf_refs_per_item(NR, variant);
 
     P_CK(S.tw.ensure(kRingLen));
@@ -294,7 +294,7 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
     const unsigned n_in = NR * net->nk, hid = net->hidden, emb = net->emb;
     const size_t row_elems = (size_t)NR * kSlots;
     const unsigned tex = texture_images(dev, D);
-    const int variant = ccf_variant(NR, true);
+    const int variant = ccf_variant(NR, true, Sn);
     const unsigned qt = ccf_refs_per_item(NR, variant);
 
     P_CK(S.tw.ensure(kRingLen));

@@ -46,7 +46,8 @@ EXPORTS = (
     "gpuisac_align_proposals_device", "gpuisac_nn_features", "gpuisac_nn_gemm", "gpuisac_nn_bias_act",
     "gpuisac_nn_relu_backward", "gpuisac_nn_colsum", "gpuisac_nn_l2norm", "gpuisac_nn_l2norm_backward",
     "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
-    "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device",
+    "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
+    "gpuisac_ccf_tile_name",
 )
 
 
@@ -114,6 +115,10 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_align_proposals_device.argtypes = [aln_cfg_ptr, vp, vp, vp, vp, cu, vp, cu, vp, vp, vp]
     L.gpuisac_nn_features.argtypes = [vp, cu, cu, cu, vp, vp, vp, vp]
     L.gpuisac_nn_col_stats.argtypes = [vp, cl, ci, cf, vp, vp, vp]
+    L.gpuisac_autotune_ccf.argtypes = [aln_cfg_ptr, vp, vp, cu, ctypes.c_char_p, ctypes.c_size_t, vp]
+    L.gpuisac_autotune_ccf.restype = ci
+    L.gpuisac_ccf_tile_name.argtypes = [cu, cu, ctypes.c_char_p, ctypes.c_size_t]
+    L.gpuisac_ccf_tile_name.restype = ci
     L.gpuisac_nn_affine_cols.argtypes = [vp, cl, ci, vp, vp, vp]
     L.gpuisac_nn_group_max.argtypes = [vp, cl, ci, ci, vp, vp]
     L.gpuisac_learned_align_device.argtypes = [aln_cfg_ptr, vp, vp, vp, ctypes.POINTER(GpuisacProposalNet), vp, cu,

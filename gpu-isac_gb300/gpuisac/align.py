@@ -215,3 +215,32 @@ def align_proposals_device(particles, refs, proposals, ring_num: int, shift_rng_
         _lib.check(L)
         raise GpuIsacError(f"gpuisac_align_proposals_device failed ({rc})")
     return d, pk
+
+
+def autotune_ccf(particles, refs, ring_num: int, shift_rng_x: float, shift_rng_y: float, shift_step: float = 1.0,
+                 n_sample: int = 2048, stream=None) -> str:
+    """Time the CCF launch's tile shapes on a sample of these stacks and keep
+    the fastest for this ring count and shift count (gpuisac_autotune_ccf).
+    Returns the tuner's report line."""
+    import torch
+
+    particles = particles.contiguous().float()
+    refs = refs.contiguous().float()
+    P, D = particles.shape[0], particles.shape[1]
+    cfg = make_config(P, refs.shape[0], D, ring_num, 256, shift_step, shift_rng_x, shift_rng_y)
+    buf = ctypes.create_string_buffer(2048)
+    st = stream if stream is not None else torch.cuda.current_stream(particles.device)
+    L = _lib.load()
+    rc = L.gpuisac_autotune_ccf(ctypes.byref(cfg), particles.data_ptr(), refs.data_ptr(), n_sample, buf, len(buf),
+                                st.cuda_stream)
+    if rc:
+        _lib.check(L)
+        raise GpuIsacError(f"gpuisac_autotune_ccf failed ({rc})")
+    return buf.value.decode()
+
+
+def ccf_tile_name(ring_num: int, n_shift: int) -> str:
+    """The tile shape CCF launches of this ring count and shift count use."""
+    buf = ctypes.create_string_buffer(64)
+    _lib.load().gpuisac_ccf_tile_name(ring_num, n_shift, buf, len(buf))
+    return buf.value.decode()

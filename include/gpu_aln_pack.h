@@ -213,6 +213,20 @@ int gpuisac_learned_align_device(const AlignConfig *cfg, const float *sbj, const
                                  float gap_margin, int *best_ref, float *best_peak, float *best_param,
                                  float *best_gap, unsigned int *fallback, unsigned long long *pairs, void *stream);
 
+/* No counterpart in the reference.  Autotuner of the CCF launch's tile shape
+ * (kernel variant, contraction warps, particles per work item): times every
+ * candidate on the first n_sample particles (0: 2048) of the device stacks
+ * through gpuisac_multi_ref_align_device and keeps the fastest for cfg's ring
+ * count and shift count for the rest of the process; every candidate gives
+ * bit-identical results.  report (optional) receives one line: each
+ * candidate's time and the choice.  Blocks until done.  Returns 0 or an error
+ * code. */
+int gpuisac_autotune_ccf(const AlignConfig *cfg, const float *sbj, const float *ref, unsigned int n_sample,
+                         char *report, size_t report_len, void *stream);
+/* No counterpart in the reference.  The tile shape the CCF launches of this
+ * ring count and shift count use, as text ("ws8/ppc8"). */
+int gpuisac_ccf_tile_name(unsigned int ring_num, unsigned int n_shift, char *buf, size_t len);
+
 /* ---- learned reference proposal (no counterpart in the reference): kernels
  * of a small embedding network, all on caller-owned row-major FP32 device
  * arrays, asynchronous on `stream`; each returns 0, or 2 for bad arguments,
