@@ -417,9 +417,11 @@ def bench_ours(args):
     # tile shape of the CCF launches: the autotuner times the candidates on a
     # sample of this workload (setup, untimed)
     from gpuisac.align import autotune_ccf
-    t0 = time.perf_counter()
-    tune_report = autotune_ccf(parts_d, refs_d, w["rings"], 3.0, 3.0, n_sample=2048, stream=stream)
-    tune = {"seconds": time.perf_counter() - t0, "report": tune_report}
+    tune = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        tune_report = autotune_ccf(parts_d, refs_d, w["rings"], 3.0, 3.0, n_sample=2048, stream=stream)
+        tune = {"seconds": time.perf_counter() - t0, "report": tune_report}
 
     for _ in range(args.warmup):
         step()
@@ -564,6 +566,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-search comparison")
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped-launch comparison")
+    ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])
     args = ap.parse_args()
