@@ -43,10 +43,23 @@ sys.path.insert(0, os.path.join(ROOT, "gpu-isac_gb300"))
 
 import numpy as np  # noqa: E402
 
-METRIC = "particle x ref alignments/s (exhaustive: 49 shifts x 256 angles x 2 mirrors)"
+METRIC = "particle x ref alignments/s (exhaustive: {S} shifts x 256 angles x 2 mirrors)"
+
+
+def metric() -> str:
+    return METRIC.format(S=WORKLOAD["n_shifts"])
 UNIT = "alignments/s"
-WORKLOAD = dict(workload="mref_50000x76_200ref", particles=50000, refs=200, img_dim=76, rings=35,
-                ring_len=256, shift_range=3, shift_step=1.0, n_shifts=49, mirror=True, snr=0.05)
+# the alignment workloads (one per --workload): plain exhaustive search
+WORKLOADS = {
+    "mref": dict(workload="mref_50000x76_200ref", particles=50000, refs=200, img_dim=76, rings=35, ring_len=256,
+                 shift_range=3, shift_step=1.0, n_shifts=49, mirror=True, snr=0.05, blob_radius=34.0, seed_idx=1),
+    "cpu2000": dict(workload="cpu_2000x64_16ref", particles=2000, refs=16, img_dim=64, rings=29, ring_len=256,
+                    shift_range=2, shift_step=1.0, n_shifts=25, mirror=True, snr=0.1, blob_radius=28.0, seed_idx=0),
+    "largebox": dict(workload="largebox_200000x128_500ref", particles=200000, refs=500, img_dim=128, rings=61,
+                     ring_len=256, shift_range=4, shift_step=1.0, n_shifts=81, mirror=True, snr=0.03,
+                     blob_radius=60.0, seed_idx=4),
+}
+WORKLOAD = WORKLOADS["mref"]
 FALLBACK_HBM_GBS = 6800.0
 FALLBACK_BF16_TFLOPS = 1900.0
 
@@ -151,7 +164,8 @@ def cpu_oracle_rate(parts, refs, target_s=15.0, threads=None):
     w = WORKLOAD
 
     def run(n):
-        cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, 3.0, 3.0)
+        sr = float(w["shift_range"])
+        cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, sr, sr)
         lay = oracle.reference_layout(cfg)
         t = time.perf_counter()
         oracle.multi_ref_align(cfg, lay, parts[:n], refs, precision="f32", threads=threads)
@@ -170,8 +184,9 @@ def bench_reference(args):
     if rank != 0:
         return
     from gpuisac import synth
-    st = synth.make_stack(args.cpu_particles, WORKLOAD["img_dim"], WORKLOAD["refs"], WORKLOAD["shift_range"],
-                          WORKLOAD["snr"], 34.0, synth.SEED_BASE + 1)
+    st = synth.make_stack(min(args.cpu_particles, WORKLOAD["particles"]), WORKLOAD["img_dim"], WORKLOAD["refs"],
+                          WORKLOAD["shift_range"], WORKLOAD["snr"], WORKLOAD["blob_radius"],
+                          synth.SEED_BASE + WORKLOAD["seed_idx"])
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
@@ -181,7 +196,8 @@ def bench_reference(args):
     # size one step to ~args.step_seconds of CPU work
     rate, n_cal, t_cal, _ = cpu_oracle_rate(st.particles, st.refs, target_s=3.0, threads=threads)
     n = int(max(threads, min(st.particles.shape[0], rate * args.step_seconds / R)))
-    cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, 3.0, 3.0)
+    sr = float(w["shift_range"])
+    cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, sr, sr)
     lay = oracle.reference_layout(cfg)
     times = []
     for i in range(args.warmup + args.steps):
@@ -193,7 +209,7 @@ def bench_reference(args):
     ms = 1000.0 * statistics.mean(times)
     value = n * R / (ms / 1000.0)
     sample = f"{n} of {w['particles']} particles x {R} refs per step (FP32 oracle port, OpenMP)"
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": metric(), "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantoms)",
             "config": dict(WORKLOAD, sample_particles=n, l2="cpu run"),
@@ -203,11 +219,16 @@ def bench_reference(args):
     print(json.dumps(line), flush=True)
 
 
-LEARNED = dict(workload="learned_100000x76_500ref", particles=100000, refs=500, train_alignments=200000,
+LEARNED = dict(workload="learned_100000x76_500ref", synth_idx=3, particles=100000, refs=500, train_alignments=200000,
                img_dim=76, rings=35, shift_range=3, n_shifts=49, snr=0.05, k=32, max_wrong=3e-3)
+# the large-box workload with the learned proposal in front (evaluation
+# particles = the workload's own, training particles an independent draw)
+LEARNED_LARGEBOX = dict(workload="largebox_learned_x128_500ref", synth_idx=4, particles=None, refs=500,
+                        train_alignments=50000, img_dim=128, rings=61, shift_range=4, n_shifts=81, snr=0.03, k=32,
+                        max_wrong=3e-3)
 
 
-def bench_learned(args, dev, L):
+def bench_learned(args, dev, L, spec=None):
     """The learned search against the plain FP32 full search on the learned
     workload: 100,000 held-out particles x 500 references, the network
     trained (untimed) on 200,000 particles the full search labelled.  Both
@@ -217,13 +238,13 @@ def bench_learned(args, dev, L):
 
     from gpuisac import learned, synth
     from gpuisac.align import multi_ref_align_device
-    w = LEARNED
-    P = args.learned_particles
-    n_train = args.learned_train
+    w = spec or LEARNED
+    P = args.learned_particles if spec is None else (w["particles"] or args.particles)
+    n_train = args.learned_train if spec is None else (args.learned_train_largebox or w["train_alignments"])
     R, NR, s = w["refs"], w["rings"], float(w["shift_range"])
     t0 = time.perf_counter()
-    tr = synth.workload_stack(3, n_particles=n_train, n_refs=R, split=1)
-    ev = synth.workload_stack(3, n_particles=P, n_refs=R)
+    tr = synth.workload_stack(w["synth_idx"], n_particles=n_train, n_refs=R, split=1)
+    ev = synth.workload_stack(w["synth_idx"], n_particles=P, n_refs=R)
     t_gen = time.perf_counter() - t0
     refs = torch.from_numpy(tr.refs).to(dev)
     tp = torch.from_numpy(tr.particles).to(dev)
@@ -358,11 +379,14 @@ def precision_vs_fp64(dev, n=64, R=200):
     import oracle
     oracle.build()
     w = WORKLOAD
-    st = synth.make_stack(n, w["img_dim"], R, w["shift_range"], w["snr"], 34.0, synth.SEED_BASE + 1)
+    R = min(R, w["refs"])
+    sr = float(w["shift_range"])
+    st = synth.make_stack(n, w["img_dim"], R, w["shift_range"], w["snr"], w["blob_radius"],
+                          synth.SEED_BASE + w["seed_idx"])
     d, pk = multi_ref_align_device(torch.from_numpy(st.particles).to(dev), torch.from_numpy(st.refs).to(dev),
-                                   w["rings"], 3.0, 3.0)
+                                   w["rings"], sr, sr)
     d, pk = d.cpu().numpy(), pk.cpu().numpy()
-    cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, 3.0, 3.0)
+    cfg = oracle.make_cfg(n, R, w["img_dim"], w["rings"], 256, 1.0, sr, sr)
     lay = oracle.reference_layout(cfg)
     t = time.perf_counter()
     _, od = oracle.multi_ref_align(cfg, lay, st.particles, st.refs, precision="f64", threads=cpu_threads())
@@ -370,7 +394,7 @@ def precision_vs_fp64(dev, n=64, R=200):
     od = np.asarray(od, np.float64).reshape(R, n)
     rel = np.abs(d - od) / np.maximum(np.abs(od), 1e-30)
     same = d.argmax(0) == od.argmax(0)
-    return {"sample": f"{n} particles x {R} refs, mref workload shape", "max_rel_peak_err": float(rel.max()),
+    return {"sample": f"{n} particles x {R} refs, {w['workload']} shape", "max_rel_peak_err": float(rel.max()),
             "median_rel_peak_err": float(np.median(rel)), "same_best_ref": float(same.mean()),
             "oracle_seconds": t}
 
@@ -392,15 +416,16 @@ def bench_ours(args):
     L = _lib.load()
     w = WORKLOAD
     P = args.particles
-    st = synth.make_stack(P, w["img_dim"], w["refs"], w["shift_range"], w["snr"], 34.0,
-                          synth.SEED_BASE + 1 + 1000 * rank)
+    st = synth.make_stack(P, w["img_dim"], w["refs"], w["shift_range"], w["snr"], w["blob_radius"],
+                          synth.SEED_BASE + w["seed_idx"] + 1000 * rank)
+    sr = float(w["shift_range"])
     R = st.refs.shape[0]
     parts_d = torch.from_numpy(st.particles).to(dev)
     refs_d = torch.from_numpy(st.refs).to(dev)
     base_d = torch.zeros((P, 2), dtype=torch.float32, device=dev)
     d_out = torch.empty((R, P), dtype=torch.float32, device=dev)
     peak_out = torch.empty((R, P, 4), dtype=torch.float32, device=dev)
-    cfg = make_config(P, R, w["img_dim"], w["rings"], 256, 1.0, 3.0, 3.0)
+    cfg = make_config(P, R, w["img_dim"], w["rings"], 256, 1.0, sr, sr)
     stream = torch.cuda.Stream(dev)
 
     def step():
@@ -420,7 +445,7 @@ def bench_ours(args):
     tune = None
     if not args.no_autotune:
         t0 = time.perf_counter()
-        tune_report = autotune_ccf(parts_d, refs_d, w["rings"], 3.0, 3.0, n_sample=2048, stream=stream)
+        tune_report = autotune_ccf(parts_d, refs_d, w["rings"], sr, sr, n_sample=2048, stream=stream)
         tune = {"seconds": time.perf_counter() - t0, "report": tune_report}
 
     for _ in range(args.warmup):
@@ -528,21 +553,23 @@ def bench_ours(args):
                "sample": f"{n} particles x {R} refs of the same workload, {t:.1f} s (FP32 oracle, OpenMP)"}
 
     prec = learned_blk = grouped_blk = None
+    learned_spec = LEARNED_LARGEBOX if WORKLOAD["workload"].startswith("largebox") else None
     if rank == 0 and world == 1 and not args.no_grouped:
         del d_out, peak_out
         torch.cuda.empty_cache()
         grouped_blk = bench_grouped(args, dev, L, parts_d, refs_d)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        prec = precision_vs_fp64(dev, n=64 if WORKLOAD["workload"].startswith("mref") else 16)
     if rank == 0 and world == 1 and not args.no_learned:
         del parts_d
         torch.cuda.empty_cache()
-        prec = precision_vs_fp64(dev)
-        learned_blk = bench_learned(args, dev, L)
+        learned_blk = bench_learned(args, dev, L, learned_spec)
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        line = {"metric": metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantoms, 50k particles/GPU)",
-                "config": dict(WORKLOAD, path="plain FP32 CUDA-core contraction", autotune=tune,
+                "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded phantoms, {P} particles/GPU)",
+                "config": dict(WORKLOAD, particles=P, path="plain FP32 CUDA-core contraction", autotune=tune,
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk}
@@ -557,7 +584,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--particles", type=int, default=WORKLOAD["particles"])
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mref",
+                    help="mref: 50,000 x 76^2 vs 200 refs (default); cpu2000: 2,000 x 64^2 vs 16; "
+                         "largebox: 128^2 particles vs 500 refs, 61 rings, 81 shifts")
+    ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -569,7 +599,16 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])
+    ap.add_argument("--learned-train-largebox", type=int, default=None)
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = WORKLOADS[args.workload]
+    if args.particles is None:
+        args.particles = WORKLOAD["particles"]
+    if args.workload != "mref":
+        # the grouped and learned blocks are defined on the 76^2 workloads
+        args.no_grouped = True
+        args.no_learned = args.no_learned or args.workload == "cpu2000"
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

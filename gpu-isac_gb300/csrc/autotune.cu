@@ -86,7 +86,8 @@ extern "C" int gpuisac_autotune_ccf(const AlignConfig* cfg, const float* sbj, co
         for (unsigned ppc : ppcs) {
             cand.push_back({kCcfWs, 8, ppc});
             cand.push_back({kCcfWs, 4, ppc});
-            cand.push_back({kCcfTmem, 8, ppc});
+            if (ccf_tile_allows_tmem(geo.NR))
+                cand.push_back({kCcfTmem, 8, ppc});
         }
     } else {
         for (unsigned ppc : ppcs)

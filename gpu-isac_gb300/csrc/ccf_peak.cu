@@ -174,26 +174,26 @@ __device__ __forceinline__ bool nbar_and(int id, int n, bool p)
                  : "memory");
     return r != 0;
 }
-// the barrier of the 256 threads that run the FFT / peak phase
-template <int BAR>
+// the barrier of the N threads that run the FFT / peak phase
+template <int BAR, int N = 256>
 __device__ __forceinline__ void phase_sync()
 {
     if (BAR == 0)
         __syncthreads();
     else
-        nbar_sync(BAR, 256);
+        nbar_sync(BAR, N);
 }
 
 // merge the nsi shift slots of each of the qt references and write the
-// outputs of particle p (the 256 threads of the FFT phase call, synchronised
+// outputs of particle p (the N threads of the FFT phase call, synchronised
 // by barrier BAR; threads < qt write)
-template <int BAR = 0>
+template <int BAR = 0, int N = 256>
 __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st, int tid, int g, int l, int qt,
                                             int nsi, unsigned q0, unsigned n_ref, unsigned n_shift, unsigned pg,
                                             unsigned p_total, const float2* shifts_f, const float2* base,
                                             float* d_out, float4* peak_out)
 {
-    phase_sync<BAR>();
+    phase_sync<BAR, N>();
     if (l == 0) {
         slots[g].v = st.bv;
         slots[g].h = st.bh;
@@ -201,7 +201,7 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
     }
     if (l < 7)
         slots[g].nb[l] = st.nb;
-    phase_sync<BAR>();
+    phase_sync<BAR, N>();
     if (tid < qt && q0 + tid < n_ref) {
         int best = tid;
         for (int i = 1; i < nsi; i++) {
@@ -220,7 +220,7 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
         d_out[o] = ps.v;
         peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
     }
-    phase_sync<BAR>();
+    phase_sync<BAR, N>();
 }
 
 // ---- mbarrier + bulk async copy (inline PTX) ----
@@ -579,23 +579,27 @@ constexpr int kWsBarFull = 2;  // + buffer: 2, 3
 constexpr int kWsBarEmpty = 4; // + buffer: 4, 5
 constexpr int kWsBarF = 6;     // FFT side only (256 threads)
 
-// CW contraction warps (4: one thread per slot k with all 4 shifts; 8: two
-// threads per slot k with 2 shifts each) + 8 FFT warps
-template <int CW>
-__global__ void __launch_bounds__(32 * CW + 256, 1)
+// CW contraction warps (slot k x NSI*128/(32 CW) shifts per thread) + one
+// 16-thread FFT group per pair of the shift group (NSI shifts x 4 references).
+// NSI = 4 up to kTmaMaxRings rings; NSI = 2 halves the staging area for up
+// to kWsMaxRings rings (the references' tensor-memory columns bound both).
+template <int CW, int NSI>
+__global__ void __launch_bounds__(32 * CW + NSI * 64, 1)
 ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift,
                    const float2* __restrict__ shifts_f, unsigned* __restrict__ err)
 {
-    constexpr int QT = 4, NSI = 4;
-    constexpr int NC = 32 * CW;        // contraction threads
-    constexpr int NT = NC + 256;       // all threads
+    constexpr int QT = 4;
+    constexpr int NP = NSI * QT;        // pairs per shift group
+    constexpr int NC = 32 * CW;         // contraction threads
+    constexpr int NF = 16 * NP;         // FFT / peak threads
+    constexpr int NT = NC + NF;         // all threads
     constexpr int SPT = NSI * 128 / NC; // shifts per contraction thread
-    static_assert(CW == 4 || CW == 8, "4 or 8 contraction warps");
+    static_assert((CW == 4 || CW == 8) && (NSI == 2 || NSI == 4) && SPT >= 1, "tile shape");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned nrp = 2 * ((ring_num + 1) / 2); // rings per staged shift (one zero ring if odd)
     float2* sbuf = reinterpret_cast<float2*>(smem_raw);                // [NSI][nrp][kSlots]
-    float2* zbuf = sbuf + (size_t)NSI * nrp * kSlots;                  // [2][16][kPairStride]
-    float2* tw = zbuf + 2 * 16 * kPairStride;                          // [256]
+    float2* zbuf = sbuf + (size_t)NSI * nrp * kSlots;                  // [2][NP][kPairStride]
+    float2* tw = zbuf + 2 * NP * kPairStride;                          // [256]
     PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + kRingLen);      // [16]
     uint64_t* bar = reinterpret_cast<uint64_t*>(slots + 16);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
@@ -769,7 +773,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                         }
                     }
                     // ---- hand the pair spectra to the FFT side ----
-                    float2* zb = zbuf + (size_t)b * 16 * kPairStride;
+                    float2* zb = zbuf + (size_t)b * NP * kPairStride;
                     nbar_sync(kWsBarEmpty + b, NT);
 #pragma unroll
                     for (int ii = 0; ii < SPT; ii++)
@@ -823,7 +827,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                         failed = true;
                         break;
                     }
-                    float2* gz = zbuf + (size_t)b * 16 * kPairStride + g * kPairStride;
+                    float2* gz = zbuf + (size_t)b * NP * kPairStride + g * kPairStride;
                     const unsigned s = s0 + g_shift;
                     if (s < n_shift)
                         fft_peak(gz, tw, l, gmask, s, n_shift, st);
@@ -832,7 +836,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                 }
                 if (failed)
                     break;
-                merge_write<kWsBarF>(slots, st, ftid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p,
+                merge_write<kWsBarF, NF>(slots, st, ftid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p,
                                      grp.p_total, shifts_f, grp.base, grp.d_out, grp.peak_out);
             }
             if (failed || !has_next)
@@ -993,11 +997,33 @@ static size_t tma_smem_bytes(unsigned ring_num)
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16;
 }
 
+// rings the warp-specialised kernel takes with 2 shifts per group: the 4
+// references' (u, v) columns of every ring fill the 512 tensor-memory columns
+constexpr unsigned kWsMaxRings = 64;
+
+static unsigned ws_shifts_per_group(unsigned ring_num) { return ring_num <= kTmaMaxRings ? 4u : 2u; }
+
 static size_t ws_smem_bytes(unsigned ring_num)
 {
-    unsigned nrp = 2 * ((ring_num + 1) / 2);
-    return (size_t)4 * nrp * kSlots * sizeof(float2) + 2 * 16 * kPairStride * sizeof(float2) +
+    const unsigned nrp = 2 * ((ring_num + 1) / 2), nsi = ws_shifts_per_group(ring_num);
+    return (size_t)nsi * nrp * kSlots * sizeof(float2) + 2 * nsi * 4 * kPairStride * sizeof(float2) +
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16;
+}
+
+template <int CW, int NSI>
+static cudaError_t launch_ws(const CcfWork& w, unsigned grid, const float2* twiddle, unsigned ring_num,
+                             unsigned n_shift, const float2* shifts_f, unsigned* err, cudaStream_t stream)
+{
+    static int configured = 0;
+    if (!configured) {
+        cudaError_t e = set_max_smem(ccf_peak_ws_kernel<CW, NSI>);
+        if (e != cudaSuccess)
+            return e;
+        configured = 1;
+    }
+    ccf_peak_ws_kernel<CW, NSI><<<grid, 32 * CW + NSI * 64, ws_smem_bytes(ring_num), stream>>>(
+        w, twiddle, ring_num, n_shift, shifts_f, err);
+    return cudaSuccess;
 }
 
 // shared memory of the general kernel (references in shared memory) at any
@@ -1011,7 +1037,7 @@ size_t ccf_peak_smem_bytes(unsigned ring_num)
 
 unsigned ccf_refs_per_item(unsigned ring_num, int variant)
 {
-    if ((variant == kCcfTmem || variant == kCcfWs) && ring_num <= kTmaMaxRings)
+    if ((variant == kCcfTmem && ring_num <= kTmaMaxRings) || (variant == kCcfWs && ring_num <= kWsMaxRings))
         return 4;
     return ccf_refs_per_cta(ring_num);
 }
@@ -1042,6 +1068,8 @@ bool ccf_tile_lookup(unsigned ring_num, unsigned n_shift, CcfTile& t)
 
 void ccf_tile_force(const CcfTile* t) { t_forced = t; }
 
+bool ccf_tile_allows_tmem(unsigned ring_num) { return ring_num <= kTmaMaxRings; }
+
 unsigned ccf_tile_generation() { return g_tile_gen.load(); }
 
 CcfTile ccf_tile(unsigned ring_num, unsigned n_shift, bool aligned)
@@ -1064,8 +1092,10 @@ CcfTile ccf_tile(unsigned ring_num, unsigned n_shift, bool aligned)
     const char* cw = getenv("GPUISAC_CCF_WS_WARPS");
     if (cw && (strcmp(cw, "4") == 0 || strcmp(cw, "8") == 0))
         t.ws_warps = cw[0] - '0';
-    if (ring_num > kTmaMaxRings || !aligned)
+    if (!aligned || ring_num > kWsMaxRings)
         t.variant = kCcfGeneral;
+    else if (ring_num > kTmaMaxRings && t.variant == kCcfTmem)
+        t.variant = kCcfWs; // the single-phase kernel stages 4 shifts: up to kTmaMaxRings rings
     if (t.ws_warps != 4)
         t.ws_warps = 8;
     if (t.ppc == 0)
@@ -1100,27 +1130,16 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* tw
         return cudaSuccess;
     const unsigned grid = persistent_grid(w.n_items, 1);
     if (variant == kCcfWs) {
-        if (ccf_tile(ring_num, n_shift, true).ws_warps == 4) {
-            static int configured = 0;
-            if (!configured) {
-                cudaError_t e = set_max_smem(ccf_peak_ws_kernel<4>);
-                if (e != cudaSuccess)
-                    return e;
-                configured = 1;
-            }
-            ccf_peak_ws_kernel<4><<<grid, 384, ws_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift,
-                                                                                 shifts_f, err);
-        } else {
-            static int configured = 0;
-            if (!configured) {
-                cudaError_t e = set_max_smem(ccf_peak_ws_kernel<8>);
-                if (e != cudaSuccess)
-                    return e;
-                configured = 1;
-            }
-            ccf_peak_ws_kernel<8><<<grid, 512, ws_smem_bytes(ring_num), stream>>>(w, twiddle, ring_num, n_shift,
-                                                                                 shifts_f, err);
-        }
+        const bool four = ccf_tile(ring_num, n_shift, true).ws_warps == 4;
+        cudaError_t e;
+        if (ring_num <= kTmaMaxRings)
+            e = four ? launch_ws<4, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream)
+                     : launch_ws<8, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+        else
+            e = four ? launch_ws<4, 2>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream)
+                     : launch_ws<8, 2>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+        if (e != cudaSuccess)
+            return e;
     } else if (variant == kCcfTmem) {
         static int configured = 0;
         if (!configured) {

@@ -88,6 +88,7 @@ CcfTile ccf_tile(unsigned ring_num, unsigned n_shift, bool aligned);
 void ccf_tile_record(unsigned ring_num, unsigned n_shift, const CcfTile& t);
 void ccf_tile_force(const CcfTile* t); // this thread only; nullptr clears
 bool ccf_tile_lookup(unsigned ring_num, unsigned n_shift, CcfTile& t);
+bool ccf_tile_allows_tmem(unsigned ring_num); // the single-phase tensor-memory kernel takes this ring count
 // bumped whenever a choice is recorded (cached launch graphs compare it)
 unsigned ccf_tile_generation();
 

@@ -129,19 +129,23 @@ def test_repeated_calls_are_identical(gpulib, cuda, small_case):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
-@pytest.mark.parametrize("NR", [29, 35, 36, 3])
-def test_ccf_kernel_variants_agree(gpulib, cuda, oracle_mod, NR, monkeypatch):
-    """The warp-specialised kernel (default), the single-phase tensor-memory
-    kernel and the general kernel: the first two run the same arithmetic in
-    the same order (bit-identical), the general one sums the rings in another
-    order (tolerance)."""
+@pytest.mark.parametrize("D,NR", [(76, 29), (76, 35), (76, 36), (76, 3), (96, 45), (128, 61)])
+def test_ccf_kernel_variants_agree(gpulib, cuda, oracle_mod, D, NR, monkeypatch):
+    """The warp-specialised kernel with 8 and 4 contraction warps (4 shifts
+    per group up to 36 rings, 2 beyond), the single-phase tensor-memory kernel
+    (up to 36 rings) and the general kernel: all but the last run the same
+    arithmetic in the same order (bit-identical), the general one sums the
+    rings in another order (tolerance)."""
     from gpuisac import multi_ref_align
-    st = synth.make_stack(70, 76, 9, 3, 0.05, 34.0, 41)
+    st = synth.make_stack(70, D, 9, 3, 0.05, D * 0.45, 41)
     runs = {}
-    for sel in ("", "tmem", "general"):
+    for sel, warps in (("", "8"), ("ws", "4"), ("tmem", "8"), ("general", "8")):
         monkeypatch.setenv("GPUISAC_CCF_KERNEL", sel)
+        monkeypatch.setenv("GPUISAC_CCF_WS_WARPS", warps)
         runs[sel] = multi_ref_align(st.particles, st.refs, NR, 3.0, 3.0)
     monkeypatch.delenv("GPUISAC_CCF_KERNEL")
-    assert np.array_equal(runs[""][0], runs["tmem"][0]) and np.array_equal(runs[""][1], runs["tmem"][1])
+    monkeypatch.delenv("GPUISAC_CCF_WS_WARPS")
+    for sel in ("ws", "tmem"):
+        assert np.array_equal(runs[""][0], runs[sel][0]) and np.array_equal(runs[""][1], runs[sel][1]), sel
     d0, dg = runs[""][1].astype(np.float64), runs["general"][1].astype(np.float64)
     assert (np.abs(d0 - dg) / np.maximum(np.abs(dg), 1e-30)).max() <= PEAK_RTOL

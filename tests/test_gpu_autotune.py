@@ -31,5 +31,7 @@ def test_autotune_records_a_choice_and_keeps_results(gpulib, cuda):
 
 
 def test_tile_name_default_and_wide_rings(gpulib):
-    # rings beyond the tensor-memory kernels' limit always use the general kernel
-    assert ccf_tile_name(61, 81).startswith("general/")
+    # up to 64 rings the warp-specialised kernel (2 shifts per group beyond
+    # 36 rings); beyond, the general kernel
+    assert ccf_tile_name(61, 81).startswith("ws")
+    assert ccf_tile_name(88, 81).startswith("general/")
