@@ -571,6 +571,8 @@ unsigned texture_images(int dev, unsigned dim) { return std::max(1u, texture_ima
 
 void record_error(int code, const char* msg) { set_error(code, "%s", msg); }
 
+std::vector<float2> shift_grid_of(float rx, float ry, float step) { return shift_grid(rx, ry, step); }
+
 } // namespace gpuisac
 
 // ====================================================================== C-ABI
@@ -643,16 +645,22 @@ void multi_ref_align(const float** sbj_data, const float** ref_data, float* isac
 
 void gpu_clear(void)
 {
-    std::lock_guard<std::mutex> lk(g_api_mu);
-    clear_state(g_state);
+    {
+        std::lock_guard<std::mutex> lk(g_api_mu);
+        clear_state(g_state);
+    }
+    gpuisac::prealign_clear();
 }
 
 void reset_shifts(float shift_range, float shift_step)
 {
+    // the pre-alignment session, if one is open, takes the new grid too
+    const int pre = gpuisac::prealign_reset_shifts(shift_range, shift_step);
     std::lock_guard<std::mutex> lk(g_api_mu);
     State& s = g_state;
     if (!s.cfg) {
-        set_error(E_STATE, "reset_shifts called before an init");
+        if (pre < 0)
+            set_error(E_STATE, "reset_shifts called before an init");
         return;
     }
     std::vector<float2> sf = shift_grid(shift_range, shift_range, shift_step);
@@ -706,18 +714,6 @@ static void not_built(const char* what)
     set_error(E_UNSUPPORTED, "%s: this library implements the multi-reference path only", what);
 }
 
-AlignParam* pre_align_init(unsigned int, const AlignConfig*, unsigned int)
-{
-    not_built("pre_align_init");
-    return nullptr;
-}
-bool pre_align_size_check(unsigned int, const AlignConfig*, unsigned int, float, bool)
-{
-    not_built("pre_align_size_check");
-    return false;
-}
-void pre_align_fetch(const float**, unsigned int, const char*) { not_built("pre_align_fetch"); }
-void pre_align_run(int, int) { not_built("pre_align_run"); }
 AlignParam* ref_free_alignment_2D_init(const AlignConfig*, const float**, const float**, const int*, unsigned int)
 {
     not_built("ref_free_alignment_2D_init");

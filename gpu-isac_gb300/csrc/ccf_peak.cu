@@ -73,15 +73,41 @@ __device__ float peak_angle(const float* x, unsigned tau, bool mirror)
     return angle;
 }
 
+// Reference: the pre-alignment's angle, CcfResultTable::compute_alignment_param
+// and interpolate_angle (cuda/gpu_aln_noref.cu:2463-2513, 2535-2577): the
+// parabola and the angle in double precision, stored as float; 180 degrees
+// added (and 360 taken off) for mirrors only.
+__device__ float pre_peak_angle(const float* xf, unsigned tau, bool mirror)
+{
+    double x[7];
+#pragma unroll
+    for (int i = 0; i < 7; i++)
+        x[i] = (double)xf[i];
+    const double c2 = 49. * x[0] + 6. * x[1] - 21. * x[2] - 32. * x[3] - 27. * x[4] - 6. * x[5] + 31. * x[6];
+    const double c3 = 5. * x[0] - 3. * x[2] - 4. * x[3] - 3. * x[4] + 5. * x[6];
+    const double step = 360.0 / (double)kRingLen;
+    double a = step * (double)tau;
+    if (c3 != 0.0)
+        a = a + step * (c2 / (2.0 * c3) - 4);
+    float angle = (float)(360.0 - a);
+    if (mirror) {
+        angle = (float)((double)angle + 180.0);
+        if (angle >= 360.0)
+            angle = (float)((double)angle - 360.0);
+    }
+    return angle;
+}
+
 // running best of one pair slot, replicated over its 16-thread group
 // (lanes 0..6 also hold the 7 samples around the peak)
 struct PeakState {
     float bv;
     unsigned bh, bt;
     float nb;
-    __device__ void reset()
+    __device__ void reset(unsigned rule = kPeakMref)
     {
-        bv = -3.40282e+038f;
+        // the pre-alignment's scan starts from 0 at index 0
+        bv = rule == kPeakPreAlign ? 0.f : -3.40282e+038f;
         bh = 0;
         bt = 0;
         nb = 0.f;
@@ -105,7 +131,7 @@ __device__ __forceinline__ void write_z(float2* zp, int k, float a1, float a2, f
 
 // inverse FFT of the pair in gz and the peak search of both mirrors
 __device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, unsigned gmask, unsigned s,
-                                         unsigned n_shift, PeakState& st)
+                                         unsigned n_shift, PeakState& st, unsigned rule = kPeakMref)
 {
     float2 x[16];
 #pragma unroll
@@ -113,6 +139,18 @@ __device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, un
         x[m] = gz[l + 16 * m];
     fft256_group<+1>(x, gz, tw, l, gmask);
     float* wf = reinterpret_cast<float*>(gz);
+    if (rule == kPeakPreAlign && s == 0 && st.bv == 0.f && st.bh == 0 && st.bt == 0) {
+        // the starting index (normal, shift 0, angle 0) stays the answer when
+        // no value beats 0: keep its 7 neighbours
+        __syncwarp(gmask);
+#pragma unroll
+        for (int k2 = 0; k2 < 16; k2++)
+            wf[l + 16 * k2] = x[perm16(k2)].x;
+        __syncwarp(gmask);
+        if (l < 7)
+            st.nb = wf[((unsigned)l - 3u) & (kRingLen - 1)];
+        __syncwarp(gmask);
+    }
 #pragma unroll
     for (int mir = 0; mir < 2; mir++) {
         // group maximum first; the first index is only needed when this
@@ -191,7 +229,7 @@ template <int BAR = 0, int N = 256>
 __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st, int tid, int g, int l, int qt,
                                             int nsi, unsigned q0, unsigned n_ref, unsigned n_shift, unsigned pg,
                                             unsigned p_total, const float2* shifts_f, const float2* base,
-                                            float* d_out, float4* peak_out)
+                                            float* d_out, float4* peak_out, unsigned rule = kPeakMref)
 {
     phase_sync<BAR, N>();
     if (l == 0) {
@@ -212,7 +250,8 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
         const PeakSlot& ps = slots[best];
         const bool mirror = ps.h >= n_shift;
         const unsigned sidx = mirror ? ps.h - n_shift : ps.h;
-        const float angle = peak_angle(ps.nb, ps.t, mirror);
+        const float angle =
+            rule == kPeakPreAlign ? pre_peak_angle(ps.nb, ps.t, mirror) : peak_angle(ps.nb, ps.t, mirror);
         const float bx = base ? base[pg].x : 0.f;
         const float by = base ? base[pg].y : 0.f;
         const float2 sf = shifts_f[sidx];
@@ -455,7 +494,7 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
 
         for (unsigned p = pb; p < pe && !failed; p++) {
             PeakState st;
-            st.reset();
+            st.reset(grp.rule);
             for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
                 // ---- wait for this group's spectra (bounded) ----
                 const bool ok = mbar_wait(bar, phase);
@@ -539,12 +578,12 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
                 // ---- inverse FFT + peak search, one pair per 16-thread group ----
                 const unsigned s = s0 + g_shift;
                 if (s < n_shift)
-                    fft_peak(gz, tw, l, gmask, s, n_shift, st);
+                    fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
             }
             if (failed)
                 break;
             merge_write(slots, st, tid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p, grp.p_total, shifts_f,
-                        grp.base, grp.d_out, grp.peak_out);
+                        grp.base, grp.d_out, grp.peak_out, grp.rule);
         }
         if (failed || !has_next)
             break;
@@ -819,7 +858,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
             for (unsigned p = pb; p < pe && !failed; p++) {
                 PeakState st;
-                st.reset();
+                st.reset(grp.rule);
                 for (unsigned s0 = 0; s0 < n_shift; s0 += NSI, it++) {
                     const unsigned b = it & 1u;
                     nbar_sync(kWsBarFull + b, NT);
@@ -830,14 +869,14 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     float2* gz = zbuf + (size_t)b * NP * kPairStride + g * kPairStride;
                     const unsigned s = s0 + g_shift;
                     if (s < n_shift)
-                        fft_peak(gz, tw, l, gmask, s, n_shift, st);
+                        fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
                     __threadfence_block();
                     nbar_arrive(kWsBarEmpty + b, NT);
                 }
                 if (failed)
                     break;
                 merge_write<kWsBarF, NF>(slots, st, ftid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p,
-                                     grp.p_total, shifts_f, grp.base, grp.d_out, grp.peak_out);
+                                     grp.p_total, shifts_f, grp.base, grp.d_out, grp.peak_out, grp.rule);
             }
             if (failed || !has_next)
                 break;
@@ -907,7 +946,7 @@ ccf_peak_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num
 
         for (unsigned p = pb; p < pe; p++) {
             PeakState st;
-            st.reset();
+            st.reset(grp.rule);
             for (unsigned s0 = 0; s0 < n_shift; s0 += NSI) {
                 float acc[RPT][NSI][4];
 #pragma unroll
@@ -979,10 +1018,10 @@ ccf_peak_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num
 
                 const unsigned s = s0 + g_shift;
                 if (s < n_shift)
-                    fft_peak(gz, tw, l, gmask, s, n_shift, st);
+                    fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
             }
             merge_write(slots, st, tid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p, grp.p_total, shifts_f,
-                        grp.base, grp.d_out, grp.peak_out);
+                        grp.base, grp.d_out, grp.peak_out, grp.rule);
         }
     }
 }
@@ -1178,7 +1217,7 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* tw
 cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle, unsigned ring_num,
                             unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_global0, unsigned p_total,
                             const float2* shifts_f, const float2* base, float* d_out, float4* peak_out,
-                            unsigned* err, cudaStream_t stream)
+                            unsigned* err, cudaStream_t stream, unsigned rule)
 {
     if (n_part == 0 || n_ref == 0)
         return cudaSuccess;
@@ -1203,6 +1242,7 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
     g.p_total = p_total;
     g.item_begin = 0;
     g.ref_tiles = (n_ref + qt - 1) / qt;
+    g.rule = rule;
     w.n_items = g.ref_tiles * ((n_part + w.ppc - 1) / w.ppc);
     return launch_ccf_peak_work(w, variant, twiddle, ring_num, n_shift, shifts_f, err, stream);
 }

@@ -59,7 +59,15 @@ struct CcfGroup {
     unsigned item_begin;    // first work item of the group
     unsigned ref_tiles;     // reference tiles of the group
     const unsigned* ref_idx; // rows of ref_sp holding the group's references 0..n_ref-1; null = 0..n_ref-1
+    unsigned rule;           // peak rule: kPeakMref or kPeakPreAlign
 };
+
+// Peak rules.  kPeakMref: the multi-reference search's (first strict maximum
+// from -FLT_MAX, angle with the reference's float/double mixing).
+// kPeakPreAlign: the pre-alignment's (first strict maximum from 0, so a
+// table with no positive value keeps index 0; angle from the parabola in
+// double precision).
+enum { kPeakMref = 0, kPeakPreAlign = 1 };
 
 // Work of one CCF launch: either one group (groups == null, `one`) or a
 // device table of n_groups groups ordered by item_begin.
@@ -107,6 +115,6 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
                             unsigned ring_num, unsigned n_shift, unsigned n_ref, unsigned n_part,
                             unsigned p_global0, unsigned p_total, const float2* shifts_f,
                             const float2* base, float* d_out, float4* peak_out, unsigned* err,
-                            cudaStream_t stream);
+                            cudaStream_t stream, unsigned rule = kPeakMref);
 
 } // namespace gpuisac

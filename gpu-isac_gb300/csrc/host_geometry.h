@@ -32,4 +32,12 @@ unsigned texture_images(int dev, unsigned dim);
 // Records an error for gpuisac_last_error and prints it.
 void record_error(int code, const char* msg);
 
+// The reference's shift grid (x outer, y inner, float accumulation).
+std::vector<float2> shift_grid_of(float rx, float ry, float step);
+
+// The pre-alignment session (prealign.cu): reset_shifts on it (-1 when none
+// is open, else 0 or an error code) and its release by gpu_clear.
+int prealign_reset_shifts(float shift_range, float shift_step);
+void prealign_clear();
+
 } // namespace gpuisac

@@ -91,9 +91,16 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.print_gpu_info.argtypes = [ctypes.c_uint]
     L.get_texture_limit.argtypes = [ctypes.c_uint]
     L.get_texture_limit.restype = ctypes.c_int
+    # the pre-alignment session, bound as bin/sp_isac_applications.py:86-157 binds it
+    L.pre_align_init.argtypes = [ctypes.c_uint, aln_cfg_ptr, ctypes.c_uint]
     L.pre_align_init.restype = ctypes.c_ulonglong
-    L.ref_free_alignment_2D_init.restype = ctypes.c_ulonglong
+    L.pre_align_size_check.argtypes = [ctypes.c_uint, aln_cfg_ptr, ctypes.c_uint, ctypes.c_float, ctypes.c_bool]
     L.pre_align_size_check.restype = ctypes.c_bool
+    L.pre_align_fetch.argtypes = [float_ptr_ptr, ctypes.c_uint, ctypes.c_char_p]
+    L.pre_align_fetch.restype = None
+    L.pre_align_run.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.pre_align_run.restype = None
+    L.ref_free_alignment_2D_init.restype = ctypes.c_ulonglong
     L.ref_free_alignment_2D_size_check.restype = ctypes.c_bool
     # additions
     L.gpuisac_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]

@@ -67,8 +67,8 @@ void multi_ref_align(const float **sbj_data, const float **ref_data, float *isac
 void gpu_clear(void);
 
 /* Replaces reset_shifts, cuda/gpu_aln_noref.cu:117-137: rebuilds the shift
- * grid with range (shift_range, shift_range); the number of shifts must not
- * change. */
+ * grid with range (shift_range, shift_range) for the open multi-reference
+ * and/or pre-alignment session; the number of shifts must not change. */
 void reset_shifts(float shift_range, float shift_step);
 
 /* Replaces print_gpu_info, cuda/gpu_aln_common.h:124 / gpu_aln_common.cu:180-218. */
@@ -78,19 +78,34 @@ void print_gpu_info(unsigned int device_idx);
  * images of side img_dim that fit the height of one 2D linear texture. */
 int get_texture_limit(unsigned int img_dim);
 
+/* ---- pre-alignment: every particle against one reference (the running
+ * global average), shifts accumulating in the returned AlignParam array;
+ * same call sequence as bin/sp_isac_applications.py:1455-1660 ---- */
+
+/* Replaces pre_align_init, cuda/gpu_aln_noref.h:77-81 (noref.cu:565-609):
+ * opens a session with cfg->sbj_num subject slots (the GPU batch) and
+ * returns host memory AlignParam[num_particles], all zero, ref_id 0, which
+ * the caller reads after each run (freed by gpu_clear).  NULL on error. */
+AlignParam *pre_align_init(unsigned int num_particles, const AlignConfig *aln_cfg, unsigned int cuda_device_id);
+/* Replaces pre_align_size_check, cuda/gpu_aln_noref.h:83-89: whether a batch
+ * of cfg->sbj_num subjects fits in request x the free device memory. */
+bool pre_align_size_check(unsigned int num_particles, const AlignConfig *cfg, unsigned int cuda_device_id,
+                          float request, bool verbose);
+/* Replaces pre_align_fetch, cuda/gpu_aln_noref.h:91-95: "sbj_batch" copies
+ * img_num <= cfg->sbj_num subject images into slots 0.. (later slots keep
+ * what an earlier fetch put there), "ref_batch" the one reference. */
+void pre_align_fetch(const float **img_data, unsigned int img_num, const char *batch_type);
+/* Replaces pre_align_run, cuda/gpu_aln_noref.h:97 (noref.cu:742-769): aligns
+ * the fetched subjects, slot i = particle start_idx + i, against the
+ * reference over the current shift grid around each particle's accumulated
+ * shift; updates AlignParam[start_idx .. stop_idx): shift += best shift,
+ * clamped to +-(img_dim - ring_num - 2), angle, mirror. */
+void pre_align_run(int start_idx, int stop_idx);
+
 /* ---- adjacent paths bound by the callers (present so that ctypes binding
  * succeeds; not built in this library: each records an error and returns a
  * failure value) ---- */
 
-/* Replaces pre_align_init, cuda/gpu_aln_noref.h:77-81. */
-AlignParam *pre_align_init(unsigned int num_particles, const AlignConfig *aln_cfg, unsigned int cuda_device_id);
-/* Replaces pre_align_size_check, cuda/gpu_aln_noref.h:83-89. */
-bool pre_align_size_check(unsigned int num_particles, const AlignConfig *cfg, unsigned int cuda_device_id,
-                          float request, bool verbose);
-/* Replaces pre_align_fetch, cuda/gpu_aln_noref.h:91-95. */
-void pre_align_fetch(const float **img_data, unsigned int img_num, const char *batch_type);
-/* Replaces pre_align_run, cuda/gpu_aln_noref.h:97. */
-void pre_align_run(int start_idx, int stop_idx);
 /* Replaces ref_free_alignment_2D_init, cuda/gpu_aln_noref.h:101-107. */
 AlignParam *ref_free_alignment_2D_init(const AlignConfig *aln_cfg, const float **sbj_data_list,
                                        const float **ref_data_list, const int *sbj_cid_list,

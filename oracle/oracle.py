@@ -200,3 +200,43 @@ def peak_search(ccf: np.ndarray):
     tau = ctypes.c_uint()
     lib().orc_f64_peak_search(_dp(ccf), two_s // 2, L, _fp(out), ctypes.byref(pk), ctypes.byref(tau))
     return out, pk.value, tau.value
+
+
+def pre_align_param(ccf: np.ndarray, shifts: np.ndarray, base, img_dim: int, ring_num: int):
+    """The pre-alignment's parameter update of one particle from its table
+    c[mirror][shift][tau] (FP64 restatement): first strict maximum from 0 at
+    index 0 over (mirror, shift, tau) (cu_max_idx_silly,
+    cuda/gpu_aln_noref.cu:1624-1665; the table's two padding values per block
+    are not part of the correlation and are left out), the 7-point parabola
+    and the angle in double precision (interpolate_angle, :2535-2577), the
+    shift added to the base shift in float and clamped to
+    +-(img_dim - ring_num - 2) computed in unsigned arithmetic
+    (compute_alignment_param, :2463-2513).  Returns (shift_x, shift_y, angle,
+    mirror) as float32 / bool."""
+    c = np.asarray(ccf, np.float64)
+    n_mir, S, L = c.shape
+    flat = c.reshape(-1)
+    best, idx = 0.0, 0
+    for i in range(flat.size):   # strict >, first occurrence
+        if flat[i] > best:
+            best, idx = flat[i], i
+    m, rest = divmod(idx, S * L)
+    s, tau = divmod(rest, L)
+    x = [c[m, s, (tau + i) % L] for i in range(-3, 4)]
+    c2 = 49. * x[0] + 6. * x[1] - 21. * x[2] - 32. * x[3] - 27. * x[4] - 6. * x[5] + 31. * x[6]
+    c3 = 5. * x[0] - 3. * x[2] - 4. * x[3] - 3. * x[4] + 5. * x[6]
+    step = 360.0 / float(L)
+    a = step * tau
+    if c3 != 0.0:
+        a = a + step * (c2 / (2.0 * c3) - 4)
+    angle = np.float32(360.0 - a)
+    if m:
+        angle = np.float32(float(angle) + 180.0)
+        if angle >= 360.0:
+            angle = np.float32(float(angle) - 360.0)
+    limit = np.float32((img_dim - ring_num - 2) % (1 << 32))
+    sx = np.float32(np.float32(base[0]) + np.float32(shifts[s][0]))
+    sy = np.float32(np.float32(base[1]) + np.float32(shifts[s][1]))
+    sx = min(max(sx, -limit), limit)
+    sy = min(max(sy, -limit), limit)
+    return np.float32(sx), np.float32(sy), np.float32(angle), bool(m)

@@ -104,9 +104,22 @@ def test_align_before_init_is_an_error(lib):
 def test_adjacent_paths_fail_loudly(lib):
     from gpuisac import _lib
     lib.gpuisac_clear_error()
-    assert lib.pre_align_init(10, ctypes.byref(_cfg(aln_type=b"pre_aln")), 0) == 0
+    lib.ref_free_alignment_2D.argtypes = []
+    lib.ref_free_alignment_2D.restype = None
+    lib.ref_free_alignment_2D()
     code, msg = _lib.last_error(lib)
     assert code == 4 and "multi-reference" in msg
+    lib.gpuisac_clear_error()
+
+
+def test_pre_align_run_before_init_fails(lib):
+    from gpuisac import _lib
+    lib.gpuisac_clear_error()
+    lib.pre_align_run.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib.pre_align_run.restype = None
+    lib.pre_align_run(0, 10)
+    code, msg = _lib.last_error(lib)
+    assert code == 3 and "before pre_align_init" in msg
     lib.gpuisac_clear_error()
 
 

@@ -166,3 +166,27 @@ def test_recovers_synthetic_truth(oracle_mod):
     assert (best[:, 3] == st.mirror).all()
     assert (best[:, 1:3] == st.shift).all()
     assert circ_diff(best[:, 0], st.angle).max() < 0.5
+
+
+def test_pre_align_rule_known_answers(oracle_mod):
+    """The pre-alignment's index rule: first strict maximum from 0, so a table
+    with no positive value keeps (normal, shift 0, angle 0); the shift update
+    adds in float and clamps to +-(img_dim - ring_num - 2)."""
+    shifts = oracle_mod.shift_array(1.0, 1.0, 1.0)
+    c = -np.ones((2, 9, 256))
+    sx, sy, ang, mir = oracle_mod.pre_align_param(c, shifts, (0.25, -0.5), 64, 29)
+    assert (sx, sy, mir) == (np.float32(0.25 + shifts[0][0]), np.float32(-0.5 + shifts[0][1]), False)
+    assert ang == np.float32(360.0)          # flat neighbourhood: c3 = 0
+    c = np.zeros((2, 9, 256))
+    c[1, 4, 10] = 5.0
+    c[1, 4, 9] = c[1, 4, 11] = 4.0           # symmetric peak: no sub-step offset
+    c[0, 7, 3] = 5.0                         # a later-found equal value loses? no: normal comes first
+    sx, sy, ang, mir = oracle_mod.pre_align_param(c, shifts, (0.0, 0.0), 64, 29)
+    assert mir is False and (sx, sy) == (np.float32(shifts[7][0]), np.float32(shifts[7][1]))
+    c[0, 7, 3] = 0.0
+    sx, sy, ang, mir = oracle_mod.pre_align_param(c, shifts, (0.0, 0.0), 64, 29)
+    assert mir is True and (sx, sy) == (np.float32(shifts[4][0]), np.float32(shifts[4][1]))
+    assert abs(float(ang) - ((360.0 - 10 * 360.0 / 256) + 180.0 - 360.0)) < 1e-4
+    # clamp: limit 64 - 29 - 2 = 33
+    sx, _, _, _ = oracle_mod.pre_align_param(-np.ones((2, 9, 256)), shifts, (40.0, 0.0), 64, 29)
+    assert sx == np.float32(33.0)
