@@ -47,7 +47,7 @@ EXPORTS = (
     "gpuisac_nn_relu_backward", "gpuisac_nn_colsum", "gpuisac_nn_l2norm", "gpuisac_nn_l2norm_backward",
     "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
-    "gpuisac_ccf_tile_name",
+    "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16",
 )
 
 
@@ -131,6 +131,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_learned_align_device.argtypes = [aln_cfg_ptr, vp, vp, vp, ctypes.POINTER(GpuisacProposalNet), vp, cu,
                                                cf, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_ulonglong), vp]
     L.gpuisac_nn_gemm.argtypes = [ci, ci, ci, cf, vp, cl, cl, vp, cl, cl, cf, vp, cl, vp]
+    L.gpuisac_nn_gemm_bf16.argtypes = [ci, ci, ci, cf, vp, cl, vp, cl, vp, ci, vp, cl, vp, vp]
+    L.gpuisac_nn_gemm_bf16.restype = ci
     L.gpuisac_nn_bias_act.argtypes = [vp, vp, cl, ci, ci, vp]
     L.gpuisac_nn_relu_backward.argtypes = [vp, vp, cl, vp]
     L.gpuisac_nn_colsum.argtypes = [vp, cl, ci, vp, ci, vp]

@@ -264,6 +264,13 @@ int gpuisac_nn_group_max(const float *G, long n, int group, int cols, float *out
  * B[k*sbk + n*sbn], C row pitch ldc. */
 int gpuisac_nn_gemm(int M, int N, int K, float alpha, const float *A, long sam, long sak, const float *B, long sbk,
                     long sbn, float beta, float *C, long ldc, void *stream);
+/* C = alpha * A B^T (+ bias[n] when given, then ReLU if relu != 0) on the
+ * tensor cores: A [M][K] (pitch lda) and B [N][K] (pitch ldb) FP32, rounded
+ * to BF16 as they are staged, FP32 accumulation, C [M][N] FP32 (pitch ldc).
+ * K, lda, ldb multiples of 4 and A, B 16-byte aligned (else 2); err: device
+ * word set non-zero if a kernel gave up waiting for its own tensor-core work. */
+int gpuisac_nn_gemm_bf16(int M, int N, int K, float alpha, const float *A, long lda, const float *B, long ldb,
+                         const float *bias, int relu, float *C, long ldc, unsigned int *err, void *stream);
 /* Y[i][j] += b[j], then ReLU if relu != 0. */
 int gpuisac_nn_bias_act(float *Y, const float *b, long rows, int cols, int relu, void *stream);
 /* dY[i] = 0 where Y[i] <= 0. */
