@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -368,6 +369,12 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
             return fail(1, "network kernel launch failed in the learned search (" #expr ")"); \
     } while (0)
 
+    // the network's GEMMs on the tensor cores (BF16 operands) unless
+    // GPUISAC_NN_FP32 is set or a shape or address rules out 16-byte staging
+    auto al16 = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+    const char* fp32 = getenv("GPUISAC_NN_FP32");
+    const bool tensor_cores = !(fp32 && fp32[0] && fp32[0] != '0') && n_in % 4 == 0 && hid % 4 == 0 &&
+                              emb % 4 == 0 && al16(net->W1) && al16(net->W2) && al16(ref_emb);
     for (unsigned c0 = 0; c0 < P; c0 += chunk) {
         const unsigned n = std::min(chunk, P - c0);
         const long rows = (long)n * Sn;
@@ -376,16 +383,29 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
         // 2. standardised ring features of every (particle, shift) row
         NN_CK(gpuisac_nn_features(reinterpret_cast<const float*>(S.sbj_sp.p), (unsigned)rows, NR, net->nk, net->mu,
                                   net->inv_sd, S.X.p, st));
-        // 3. embeddings
-        NN_CK(gpuisac_nn_gemm((int)rows, (int)hid, (int)n_in, 1.f, S.X.p, n_in, 1, net->W1, 1, n_in, 0.f, S.H.p, hid,
-                              st));
-        NN_CK(gpuisac_nn_bias_act(S.H.p, net->b1, rows, (int)hid, 1, st));
-        NN_CK(gpuisac_nn_gemm((int)rows, (int)emb, (int)hid, 1.f, S.H.p, hid, 1, net->W2, 1, hid, 0.f, S.Z.p, emb,
-                              st));
-        NN_CK(gpuisac_nn_bias_act(S.Z.p, net->b2, rows, (int)emb, 0, st));
+        // 3. embeddings (BF16 tensor cores, bias and ReLU in the epilogue; FP32
+        // CUDA-core GEMMs where the shapes do not allow the 16-byte staging)
+        if (tensor_cores) {
+            NN_CK(gpuisac_nn_gemm_bf16((int)rows, (int)hid, (int)n_in, 1.f, S.X.p, n_in, net->W1, n_in, net->b1, 1,
+                                       S.H.p, hid, S.err.p, st));
+            NN_CK(gpuisac_nn_gemm_bf16((int)rows, (int)emb, (int)hid, 1.f, S.H.p, hid, net->W2, hid, net->b2, 0,
+                                       S.Z.p, emb, S.err.p, st));
+        } else {
+            NN_CK(gpuisac_nn_gemm((int)rows, (int)hid, (int)n_in, 1.f, S.X.p, n_in, 1, net->W1, 1, n_in, 0.f, S.H.p,
+                                  hid, st));
+            NN_CK(gpuisac_nn_bias_act(S.H.p, net->b1, rows, (int)hid, 1, st));
+            NN_CK(gpuisac_nn_gemm((int)rows, (int)emb, (int)hid, 1.f, S.H.p, hid, 1, net->W2, 1, hid, 0.f, S.Z.p,
+                                  emb, st));
+            NN_CK(gpuisac_nn_bias_act(S.Z.p, net->b2, rows, (int)emb, 0, st));
+        }
         NN_CK(gpuisac_nn_l2norm(S.Z.p, rows, (int)emb, S.E.p, S.nrm.p, st));
         // 4. similarity to every reference, best over shifts, top k
-        NN_CK(gpuisac_nn_gemm((int)rows, (int)R, (int)emb, 1.f, S.E.p, emb, 1, ref_emb, 1, emb, 0.f, S.G.p, R, st));
+        if (tensor_cores)
+            NN_CK(gpuisac_nn_gemm_bf16((int)rows, (int)R, (int)emb, 1.f, S.E.p, emb, ref_emb, emb, nullptr, 0, S.G.p,
+                                       R, S.err.p, st));
+        else
+            NN_CK(gpuisac_nn_gemm((int)rows, (int)R, (int)emb, 1.f, S.E.p, emb, 1, ref_emb, 1, emb, 0.f, S.G.p, R,
+                                  st));
         NN_CK(gpuisac_nn_group_max(S.G.p, n, (int)Sn, (int)R, S.Smax.p, st));
         NN_CK(gpuisac_nn_topk(S.Smax.p, n, (int)R, (int)k, S.prop.p, st));
         // 5. exhaustive search of every particle over its proposals
