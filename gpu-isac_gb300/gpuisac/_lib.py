@@ -47,7 +47,7 @@ EXPORTS = (
     "gpuisac_nn_relu_backward", "gpuisac_nn_colsum", "gpuisac_nn_l2norm", "gpuisac_nn_l2norm_backward",
     "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
-    "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16",
+    "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
 )
 
 
@@ -133,6 +133,10 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_nn_gemm.argtypes = [ci, ci, ci, cf, vp, cl, cl, vp, cl, cl, cf, vp, cl, vp]
     L.gpuisac_nn_gemm_bf16.argtypes = [ci, ci, ci, cf, vp, cl, vp, cl, vp, ci, vp, cl, vp, vp]
     L.gpuisac_nn_gemm_bf16.restype = ci
+    L.gpuisac_assign_groups_device.argtypes = [vp, ctypes.c_ulonglong, cu, cu, vp, vp, ctypes.POINTER(cu), vp]
+    L.gpuisac_assign_groups_device.restype = ci
+    L.gpuisac_assign_groups.argtypes = [vp, cu, cu, vp]
+    L.gpuisac_assign_groups.restype = ci
     L.gpuisac_nn_bias_act.argtypes = [vp, vp, cl, ci, ci, vp]
     L.gpuisac_nn_relu_backward.argtypes = [vp, vp, cl, vp]
     L.gpuisac_nn_colsum.argtypes = [vp, cl, ci, vp, ci, vp]

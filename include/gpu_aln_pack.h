@@ -292,6 +292,28 @@ int gpuisac_nn_adam(float *p, const float *g, float *m, float *v, long n, float 
 /* idx[i][0..k-1] = columns of the k largest S[i][.], best first (cols <= 1024, k <= 64). */
 int gpuisac_nn_topk(const float *S, long rows, int cols, int k, unsigned int *idx, void *stream);
 
+/* Replaces EMAN2's Util::assign_groups (util_sparx.cpp, not vendored), which
+ * bin/sp_isac2_gpu.py:1119 calls on the alignment's peak matrix right after
+ * the alignment: the equal-size assignment of nima particles to nref groups
+ * taking (reference, particle) pairs in descending peak order (equal peaks:
+ * smaller index ref*nima + particle first), maxasi = nima / nref per group, the
+ * group that closes last also taking the nima % nref particles left over.
+ * d: device array d[ref * d_pitch + particle] (d_pitch 0 = nima; the layout
+ * gpuisac_multi_ref_align_device writes), finite values; 1 <= nref <= nima,
+ * nref * nima < 2^32.  Outputs (device, either may be NULL but not both):
+ * belongsto[nima] = each particle's group; id_list_long[nima + 1] = the list
+ * Util::assign_groups returns (each group's maxasi members in descending pair
+ * order, group after group, the leftovers in descending order of their pair
+ * with the last group, then that group's index).  rounds (host, optional)
+ * receives the number of parallel proposal rounds.  Blocks until done.
+ * Returns 0, 2 (bad arguments, a NaN peak) or 1 (CUDA error). */
+int gpuisac_assign_groups_device(const float *d, unsigned long long d_pitch, unsigned int nref, unsigned int nima,
+                                 int *belongsto, int *id_list_long, unsigned int *rounds, void *stream);
+/* The same on host arrays, in Util::assign_groups' shape: d[nref * nima]
+ * (host), id_list_long[nima + 1] (host) receives the list.  Copies d to the
+ * current device and the list back.  Returns 0 or an error code. */
+int gpuisac_assign_groups(const float *d, unsigned int nref, unsigned int nima, int *id_list_long);
+
 /* Ring spectra of a device image stack at every shift of cfg's grid, as the
  * CCF kernel consumes them: out [n_img][n_shift][ring_num][128][2] (float),
  * slot 0 = (F[0], F[128]); is_ref selects the reference layout (ring weight

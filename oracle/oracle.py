@@ -40,7 +40,7 @@ def build(force: bool = False) -> str:
 def _stale() -> bool:
     t = os.path.getmtime(_LIB_PATH)
     return any(os.path.getmtime(os.path.join(_HERE, f)) > t
-               for f in ("isac_oracle.c", "isac_oracle.h", "isac_oracle_core.h"))
+               for f in ("isac_oracle.c", "isac_oracle.h", "isac_oracle_core.h", "assign_oracle.cpp"))
 
 
 def lib():
@@ -73,6 +73,8 @@ def lib():
             f.argtypes = [cfgp, layp, fp, fp, fp, fp, rp, ctypes.c_uint, ctypes.c_int]
         L.orc_f64_peak_search.argtypes = [dp, ctypes.c_uint, ctypes.c_uint, fp, dp,
                                           ctypes.POINTER(ctypes.c_uint)]
+        L.orc_assign_groups.argtypes = [fp, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(ctypes.c_int)]
+        L.orc_assign_groups.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -240,3 +242,38 @@ def pre_align_param(ccf: np.ndarray, shifts: np.ndarray, base, img_dim: int, rin
     sx = min(max(sx, -limit), limit)
     sy = min(max(sy, -limit), limit)
     return np.float32(sx), np.float32(sy), np.float32(angle), bool(m)
+
+
+def assign_groups(d: np.ndarray, nref: int, nima: int) -> np.ndarray:
+    """The equal-size group assignment on d[ref * nima + particle]
+    (assign_oracle.cpp restates EMAN2's Util::assign_groups, which
+    bin/sp_isac2_gpu.py:1119 calls): returns id_list_long, nima + 1 ints."""
+    d = np.ascontiguousarray(np.asarray(d, np.float32).reshape(-1))
+    if d.size != nref * nima:
+        raise ValueError("d must hold nref * nima peaks")
+    out = np.zeros(nima + 1, np.int32)
+    rc = lib().orc_assign_groups(_fp(d), nref, nima, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    if rc:
+        raise ValueError(f"oracle assign_groups rejected its input ({rc})")
+    return out
+
+
+def belongsto_from_id_list(id_list_long, numref: int, nima: int) -> np.ndarray:
+    """The caller's reading of the assignment (bin/sp_isac2_gpu.py:1121-1136):
+    the first maxasi * numref entries fill the groups maxasi at a time, the
+    next nima % maxasi entries join the group named by the last entry, and
+    belongsto[particle] is its group.  (When nima % numref >= maxasi the
+    caller reads fewer extras than the assignment lists and those particles
+    keep group 0; that is the caller's arithmetic, restated as it is.)"""
+    ids = [int(x) for x in id_list_long]
+    maxasi = nima // numref
+    groups = [[] for _ in range(numref)]
+    for i in range(maxasi * numref):
+        groups[i // maxasi].append(ids[i])
+    for i in range(nima % maxasi):
+        groups[ids[-1]].append(ids[maxasi * numref + i])
+    belongsto = np.zeros(nima, np.int32)
+    for k in range(numref):
+        for i in sorted(groups[k]):
+            belongsto[i] = k
+    return belongsto

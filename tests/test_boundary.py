@@ -127,3 +127,17 @@ def test_python_host_raises_without_library(tmp_path):
     from gpuisac import _lib
     with pytest.raises(_lib.GpuIsacError):
         _lib.load(str(tmp_path / "missing.so"))
+
+
+def test_assign_groups_rejects_bad_arguments_on_the_host(lib):
+    from gpuisac import _lib
+    d = (ctypes.c_float * 6)()
+    out = (ctypes.c_int * 4)()
+    lib.gpuisac_clear_error()
+    assert lib.gpuisac_assign_groups(None, 2, 3, ctypes.cast(out, ctypes.c_void_p)) == 2
+    assert lib.gpuisac_assign_groups(ctypes.cast(d, ctypes.c_void_p), 0, 3, ctypes.cast(out, ctypes.c_void_p)) == 2
+    assert lib.gpuisac_assign_groups(ctypes.cast(d, ctypes.c_void_p), 4, 3, ctypes.cast(out, ctypes.c_void_p)) == 2
+    assert lib.gpuisac_assign_groups_device(ctypes.cast(d, ctypes.c_void_p), 0, 2, 3, None, None, None, None) == 2
+    code, msg = _lib.last_error(lib)
+    assert code == 2 and "assign_groups" in msg
+    lib.gpuisac_clear_error()
