@@ -368,6 +368,81 @@ def bench_grouped(args, dev, L, parts_d, refs_d):
             "data": "groups cut from the resident 50k-particle / 200-ref synthetic stacks"}
 
 
+def bench_assign(args, dev, L, d_dev, cpu=True):
+    """The equal-size group assignment ISAC runs on the alignment's peak matrix
+    (gpuisac_assign_groups_device; EMAN2's Util::assign_groups on the host in
+    the reference) on d_dev [R][P] already in HBM, L2 flushed before every
+    timed call; the host-buffer C-ABI call with d copied in and the list
+    copied out; the oracle's CPU restatement on the same d; and the
+    list compared with the oracle's."""
+    import torch
+
+    from gpuisac.assign import assign_groups_device
+    R, P = d_dev.shape
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)       # 256 MB > L2
+    ids = torch.empty(P + 1, dtype=torch.int32, device=dev)
+    bel = torch.empty(P, dtype=torch.int32, device=dev)
+    rounds = ctypes.c_uint()
+
+    def call():
+        rc = L.gpuisac_assign_groups_device(d_dev.data_ptr(), P, R, P, bel.data_ptr(), ids.data_ptr(),
+                                            ctypes.byref(rounds), stream.cuda_stream)
+        if rc:
+            _lib_check(L)
+
+    for _ in range(max(args.warmup, 3)):
+        call()
+    total = 0.0
+    steps = max(args.steps, 3)
+    launches0 = L.gpuisac_launch_count()
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    launches = (L.gpuisac_launch_count() - launches0) / steps
+    ms = total / steps
+    hbm_peak, _, peak_kind = peaks()
+    alg_bytes = 4.0 * R * P + 4.0 * P + 4.0 * (P + 1)
+    blk = {"workload": f"{P} particles x {R} groups", "ms_per_call": ms, "pairs_per_s": R * P / (ms / 1000.0),
+           "rounds": rounds.value, "kernel_launches_per_call": launches,
+           "roofline": {"bound": "hbm", "achieved": alg_bytes / (ms / 1000.0) / 1e9, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": alg_bytes / (ms / 1000.0) / 1e9 / hbm_peak,
+                        "algorithmic_bytes": alg_bytes, "peak_kind": peak_kind},
+           "l2": "256 MB buffer written before each timed call"}
+    d_host = d_dev.cpu().numpy()
+    out = np.zeros(P + 1, np.int32)
+    t0 = time.perf_counter()
+    rc = L.gpuisac_assign_groups(d_host.ctypes.data, R, P, out.ctypes.data)
+    if rc:
+        _lib_check(L)
+    t_host = time.perf_counter() - t0
+    blk["e2e"] = {"ms_per_call": 1000.0 * t_host, "h2d_bytes": 4 * R * P, "d2h_bytes": 4 * (P + 1),
+                  "api": "gpuisac_assign_groups (host d, host list)"}
+    blk["identical_to_device_call"] = bool(np.array_equal(out, ids.cpu().numpy()))
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        t0 = time.perf_counter()
+        want = oracle.assign_groups(d_host, R, P)
+        t_cpu = time.perf_counter() - t0
+        blk["cpu_baseline"] = {"ms_per_call": 1000.0 * t_cpu, "cores": 1, "kind": "port",
+                               "sample": "the whole call (std::sort of the pairs + the serial greedy)"}
+        blk["identical_to_oracle"] = bool(np.array_equal(want, out))
+    del flush
+    return blk
+
+
+def _lib_check(L):
+    from gpuisac import _lib
+    _lib.check(L)
+    raise RuntimeError("library call failed")
+
+
 def precision_vs_fp64(dev, n=64, R=200):
     """Peak values of the plain FP32 GPU path against the FP64 oracle on a
     small stack of the headline workload's shape (same stack on both)."""
@@ -552,8 +627,17 @@ def bench_ours(args):
         cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{n} particles x {R} refs of the same workload, {t:.1f} s (FP32 oracle, OpenMP)"}
 
-    prec = learned_blk = grouped_blk = None
+    prec = learned_blk = grouped_blk = assign_blk = None
     learned_spec = LEARNED_LARGEBOX if WORKLOAD["workload"].startswith("largebox") else None
+    if rank == 0 and world == 1 and not args.no_assign:
+        assign_blk = {"on_alignment_peaks": bench_assign(args, dev, L, d_out, cpu=not args.no_cpu)}
+        rng = torch.Generator(device=dev)
+        rng.manual_seed(20261203 + 5)
+        big = torch.rand((500, 100000), generator=rng, device=dev) * 0.1 + 0.5
+        cls = torch.randint(0, 500, (100000,), generator=rng, device=dev)
+        big[cls, torch.arange(100000, device=dev)] += 0.3 * torch.rand(100000, generator=rng, device=dev)
+        assign_blk["synthetic_100000x500"] = bench_assign(args, dev, L, big, cpu=False)
+        del big
     if rank == 0 and world == 1 and not args.no_grouped:
         del d_out, peak_out
         torch.cuda.empty_cache()
@@ -572,7 +656,8 @@ def bench_ours(args):
                 "config": dict(WORKLOAD, particles=P, path="plain FP32 CUDA-core contraction", autotune=tune,
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-                "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk}
+                "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk,
+                "assign_groups": assign_blk}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -596,6 +681,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-search comparison")
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped-launch comparison")
+    ap.add_argument("--no-assign", action="store_true", help="skip the group-assignment block")
     ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])

@@ -42,6 +42,8 @@ namespace {
 
 constexpr unsigned kRows = 8;         // row slices of d per particle in the proposal scan
 constexpr unsigned kSelThreads = 256; // threads of a group's selection / ranking CTA
+constexpr unsigned kSmallSel = 1024;  // groups up to this many candidates select in shared memory
+constexpr unsigned kSparseDiv = 8;    // a round with at most nima / 8 particles to place uses the list form
 constexpr unsigned kErrNaN = 1u, kErrInternal = 2u;
 
 enum { kScNext = 0, kScErr = 1, kScLast = 2, kScLeft = 3, kScCount = 4 };
@@ -54,20 +56,27 @@ __device__ __forceinline__ uint64_t pair_key(float v, uint32_t l)
 }
 
 // Each unplaced particle's best pair among the groups whose threshold it
-// beats.  Block = 32 particles x kRows row slices; lanes of a warp read 32
-// particles of one row of d (coalesced where the particles are consecutive).
+// beats.  Block = 32 consecutive particles x kRows row slices; the lanes of a
+// warp read one row of d for the block's unplaced particles, so that a round
+// with few of them touches only the 32-byte sectors they share; a block with
+// none returns at once.  redo = NULL: every particle (the first round);
+// otherwise redo[p] = 1 marks the particles turned away last round (cleared
+// here).
 __global__ void __launch_bounds__(32 * kRows)
 propose_kernel(const float* __restrict__ d, size_t pitch, unsigned nref, unsigned nima,
-               const unsigned* __restrict__ act, unsigned n_act, const uint64_t* __restrict__ theta,
-               int* __restrict__ assign, uint64_t* __restrict__ pkey, unsigned* __restrict__ cnt,
-               unsigned* __restrict__ touched, unsigned* __restrict__ err)
+               unsigned char* __restrict__ redo, const uint64_t* __restrict__ theta, int* __restrict__ assign,
+               uint64_t* __restrict__ pkey, unsigned* __restrict__ cnt, unsigned* __restrict__ touched,
+               unsigned* __restrict__ err)
 {
     __shared__ uint64_t s_key[kRows][32];
     __shared__ int s_grp[kRows][32];
     const unsigned x = threadIdx.x, y = threadIdx.y;
-    const unsigned i = blockIdx.x * 32 + x;
-    const bool live = i < n_act;
-    const unsigned p = live ? (act ? act[i] : i) : 0u;
+    const unsigned p = blockIdx.x * 32 + x;
+    const bool live = p < nima && (!redo || redo[p]);
+    if (!__syncthreads_or(live))
+        return;
+    if (live && redo && y == 0)
+        redo[p] = 0;
     uint64_t best = 0;
     int bg = -1;
     bool nan = false;
@@ -96,6 +105,56 @@ propose_kernel(const float* __restrict__ d, size_t pitch, unsigned nref, unsigne
                 best = s_key[r][x];
                 bg = s_grp[r][x];
             }
+        assign[p] = bg;
+        pkey[p] = best;
+        if (bg >= 0) {
+            atomicAdd(cnt + bg, 1u);
+            touched[bg] = 1u;
+        }
+    }
+}
+
+// The list form of the proposal scan, for rounds with few particles to
+// place: one warp per particle of list[0..n), its lanes striding over the
+// rows of the particle's column, the best pair found by a warp reduction.
+__global__ void __launch_bounds__(256)
+propose_list_kernel(const float* __restrict__ d, size_t pitch, unsigned nref, unsigned nima,
+                    const unsigned* __restrict__ list, unsigned n, unsigned char* __restrict__ redo,
+                    const uint64_t* __restrict__ theta, int* __restrict__ assign, uint64_t* __restrict__ pkey,
+                    unsigned* __restrict__ cnt, unsigned* __restrict__ touched, unsigned* __restrict__ err)
+{
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n)
+        return;
+    const unsigned p = list[i];
+    uint64_t best = 0;
+    int bg = -1;
+    bool nan = false;
+    const float* col = d + p;
+#pragma unroll 4
+    for (unsigned g = lane; g < nref; g += 32) {
+        const float v = __ldg(col + (size_t)g * pitch);
+        nan |= (v != v);
+        const uint64_t k = pair_key(v, g * nima + p);
+        if (k > best && k > __ldg(theta + g)) {
+            best = k;
+            bg = (int)g;
+        }
+    }
+#pragma unroll
+    for (unsigned o = 16; o > 0; o >>= 1) {
+        const uint64_t ok = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+        const int og = __shfl_xor_sync(0xFFFFFFFFu, bg, o);
+        if (ok > best) {
+            best = ok;
+            bg = og;
+        }
+    }
+    if (__any_sync(0xFFFFFFFFu, nan) && lane == 0)
+        atomicOr(err, kErrNaN);
+    if (lane == 0) {
+        redo[p] = 0;
         assign[p] = bg;
         pkey[p] = best;
         if (bg >= 0) {
@@ -223,14 +282,36 @@ __device__ uint64_t kth_largest(const uint64_t* __restrict__ keys, unsigned c, u
     return prefix;
 }
 
+// The k-th largest of c <= kSmallSel distinct keys: the one with exactly
+// k - 1 larger keys, counted against a copy in shared memory.
+__device__ uint64_t kth_largest_small(const uint64_t* __restrict__ keys, unsigned c, unsigned k)
+{
+    __shared__ uint64_t s_keys[kSmallSel];
+    __shared__ uint64_t s_found;
+    for (unsigned i = threadIdx.x; i < c; i += blockDim.x)
+        s_keys[i] = keys[i];
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < c; i += blockDim.x) {
+        const uint64_t v = s_keys[i];
+        unsigned larger = 0;
+        for (unsigned j = 0; j < c; j++)
+            larger += s_keys[j] > v;
+        if (larger == k - 1)
+            s_found = v;
+    }
+    __syncthreads();
+    return s_found;
+}
+
 // One CTA per group: a group with proposals and at least maxasi members keeps
 // its maxasi best, takes the maxasi-th best key as its threshold and turns
-// the others away (they propose again next round).
+// the others away: marked in redo and appended to list (they propose again
+// next round); n_next counts them.
 __global__ void __launch_bounds__(kSelThreads)
 select_kernel(unsigned maxasi, const unsigned* __restrict__ off, const unsigned* __restrict__ bp,
               const uint64_t* __restrict__ bk, unsigned* __restrict__ cnt, unsigned* __restrict__ touched,
-              uint64_t* __restrict__ theta, int* __restrict__ assign, unsigned* __restrict__ next_act,
-              unsigned* __restrict__ n_next)
+              uint64_t* __restrict__ theta, int* __restrict__ assign, unsigned char* __restrict__ redo,
+              unsigned* __restrict__ list, unsigned* __restrict__ n_next)
 {
     const unsigned g = blockIdx.x;
     const unsigned t = touched[g], c = cnt[g];
@@ -242,13 +323,14 @@ select_kernel(unsigned maxasi, const unsigned* __restrict__ off, const unsigned*
     if (c < maxasi)
         return;
     const unsigned base = off[g];
-    const uint64_t kth = kth_largest(bk + base, c, maxasi);
+    const uint64_t kth = c <= kSmallSel ? kth_largest_small(bk + base, c, maxasi) : kth_largest(bk + base, c, maxasi);
     if (c > maxasi)
         for (unsigned i = threadIdx.x; i < c; i += blockDim.x)
             if (bk[base + i] < kth) {
                 const unsigned p = bp[base + i];
                 assign[p] = -1;
-                next_act[atomicAdd(n_next, 1u)] = p;
+                redo[p] = 1;
+                list[atomicAdd(n_next, 1u)] = p;
             }
     if (threadIdx.x == 0) {
         theta[g] = kth;
@@ -390,7 +472,8 @@ struct Buf {
 struct AssignState {
     std::mutex mu;
     Buf<uint64_t> theta, pkey, bk;
-    Buf<unsigned> cnt, touched, off, fill, bp, act0, act1, sc;
+    Buf<unsigned> cnt, touched, off, fill, bp, list, sc;
+    Buf<unsigned char> redo;
     Buf<int> assign;
     Buf<float> d_host_copy;
     Buf<int> ids_host_copy;
@@ -442,8 +525,8 @@ int assign_locked(const float* d, size_t pitch, unsigned nref, unsigned nima, in
     A_CK(w.pkey.ensure(nima));
     A_CK(w.bp.ensure(nima));
     A_CK(w.bk.ensure(nima));
-    A_CK(w.act0.ensure(nima));
-    A_CK(w.act1.ensure(nima));
+    A_CK(w.redo.ensure(nima));
+    A_CK(w.list.ensure(nima));
     A_CK(w.sc.ensure(kScCount));
     if (!w.h_sc)
         A_CK(cudaHostAlloc(&w.h_sc, kScCount * sizeof(unsigned), cudaHostAllocDefault));
@@ -453,19 +536,27 @@ int assign_locked(const float* d, size_t pitch, unsigned nref, unsigned nima, in
     A_CK(cudaMemsetAsync(w.touched.p, 0, nref * sizeof(unsigned), st));
     A_CK(cudaMemsetAsync(w.sc.p, 0, kScCount * sizeof(unsigned), st));
 
+    A_CK(cudaMemsetAsync(w.redo.p, 0, nima, st));
+
     const unsigned long long max_rounds = (unsigned long long)nref * nima + 1;
-    const unsigned* act = nullptr;
-    unsigned n_act = nima, rounds = 0;
+    unsigned rounds = 0, turned = nima;
     for (;;) {
-        unsigned* next = (rounds & 1) ? w.act1.p : w.act0.p;
-        propose_kernel<<<(n_act + 31) / 32, dim3(32, kRows), 0, st>>>(d, pitch, nref, nima, act, n_act, w.theta.p,
-                                                                       w.assign.p, w.pkey.p, w.cnt.p, w.touched.p,
-                                                                       w.sc.p + kScErr);
+        // the list written by the previous round's selection is read here,
+        // before this round's selection rewrites it
+        if (rounds > 0 && turned <= nima / kSparseDiv)
+            propose_list_kernel<<<(turned + 7) / 8, 256, 0, st>>>(d, pitch, nref, nima, w.list.p, turned, w.redo.p,
+                                                                  w.theta.p, w.assign.p, w.pkey.p, w.cnt.p,
+                                                                  w.touched.p, w.sc.p + kScErr);
+        else
+            propose_kernel<<<(nima + 31) / 32, dim3(32, kRows), 0, st>>>(d, pitch, nref, nima,
+                                                                          rounds ? w.redo.p : nullptr, w.theta.p,
+                                                                          w.assign.p, w.pkey.p, w.cnt.p,
+                                                                          w.touched.p, w.sc.p + kScErr);
         offsets_kernel<<<1, 1024, 0, st>>>(nref, w.cnt.p, w.touched.p, w.off.p, w.fill.p, w.sc.p + kScNext);
         scatter_kernel<<<(nima + 255) / 256, 256, 0, st>>>(nima, w.assign.p, w.pkey.p, w.touched.p, w.off.p,
                                                            w.fill.p, w.bp.p, w.bk.p);
         select_kernel<<<nref, kSelThreads, 0, st>>>(maxasi, w.off.p, w.bp.p, w.bk.p, w.cnt.p, w.touched.p,
-                                                     w.theta.p, w.assign.p, next, w.sc.p + kScNext);
+                                                     w.theta.p, w.assign.p, w.redo.p, w.list.p, w.sc.p + kScNext);
         g_kernel_launches.fetch_add(4, std::memory_order_relaxed);
         A_CK(cudaGetLastError());
         A_CK(cudaMemcpyAsync(w.h_sc, w.sc.p, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -473,12 +564,11 @@ int assign_locked(const float* d, size_t pitch, unsigned nref, unsigned nima, in
         rounds++;
         if (w.h_sc[kScErr] & kErrNaN)
             return fail(2, "assign_groups: d holds a NaN peak");
-        n_act = w.h_sc[kScNext];
-        if (n_act == 0)
+        turned = w.h_sc[kScNext];
+        if (turned == 0)
             break;
-        if (n_act > nima || rounds >= max_rounds)
+        if (turned > nima || rounds >= max_rounds)
             return fail(1, "assign_groups: the proposal rounds did not settle (internal error)");
-        act = next;
     }
 
     last_group_kernel<<<1, 1024, 0, st>>>(nref, maxasi, w.theta.p, w.cnt.p, w.sc.p);
