@@ -650,16 +650,18 @@ void gpu_clear(void)
         clear_state(g_state);
     }
     gpuisac::prealign_clear();
+    gpuisac::multigroup_clear();
 }
 
 void reset_shifts(float shift_range, float shift_step)
 {
-    // the pre-alignment session, if one is open, takes the new grid too
+    // the pre-alignment and multigroup sessions, if open, take the new grid too
     const int pre = gpuisac::prealign_reset_shifts(shift_range, shift_step);
+    const int mg = gpuisac::multigroup_reset_shifts(shift_range, shift_step);
     std::lock_guard<std::mutex> lk(g_api_mu);
     State& s = g_state;
     if (!s.cfg) {
-        if (pre < 0)
+        if (pre < 0 && mg < 0)
             set_error(E_STATE, "reset_shifts called before an init");
         return;
     }
@@ -707,25 +709,6 @@ int get_texture_limit(unsigned int img_dim)
     cudaGetDevice(&dev);
     return (int)texture_image_limit(dev, img_dim);
 }
-
-// ---- adjacent paths: not built here ----
-static void not_built(const char* what)
-{
-    set_error(E_UNSUPPORTED, "%s: this library implements the multi-reference path only", what);
-}
-
-AlignParam* ref_free_alignment_2D_init(const AlignConfig*, const float**, const float**, const int*, unsigned int)
-{
-    not_built("ref_free_alignment_2D_init");
-    return nullptr;
-}
-bool ref_free_alignment_2D_size_check(const AlignConfig*, unsigned int, float, bool)
-{
-    not_built("ref_free_alignment_2D_size_check");
-    return false;
-}
-void ref_free_alignment_2D(void) { not_built("ref_free_alignment_2D"); }
-void ref_free_alignment_2D_filter_references(float, float) { not_built("ref_free_alignment_2D_filter_references"); }
 
 int gpuisac_shift_count(const AlignConfig* cfg)
 {

@@ -40,4 +40,8 @@ std::vector<float2> shift_grid_of(float rx, float ry, float step);
 int prealign_reset_shifts(float shift_range, float shift_step);
 void prealign_clear();
 
+// The multigroup session (multigroup.cu), likewise.
+int multigroup_reset_shifts(float shift_range, float shift_step);
+void multigroup_clear();
+
 } // namespace gpuisac

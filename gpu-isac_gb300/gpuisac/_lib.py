@@ -48,6 +48,7 @@ EXPORTS = (
     "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
+    "gpuisac_ref_free_averages",
 )
 
 
@@ -100,8 +101,16 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.pre_align_fetch.restype = None
     L.pre_align_run.argtypes = [ctypes.c_int, ctypes.c_int]
     L.pre_align_run.restype = None
+    # the multigroup session, bound as bin/sp_isac_applications.py:86-157 binds it
+    L.ref_free_alignment_2D_init.argtypes = [aln_cfg_ptr, float_ptr_ptr, float_ptr_ptr,
+                                             ctypes.POINTER(ctypes.c_int), ctypes.c_uint]
     L.ref_free_alignment_2D_init.restype = ctypes.c_ulonglong
+    L.ref_free_alignment_2D_size_check.argtypes = [aln_cfg_ptr, ctypes.c_uint, ctypes.c_float, ctypes.c_bool]
     L.ref_free_alignment_2D_size_check.restype = ctypes.c_bool
+    L.ref_free_alignment_2D.argtypes = []
+    L.ref_free_alignment_2D.restype = None
+    L.ref_free_alignment_2D_filter_references.argtypes = [ctypes.c_float, ctypes.c_float]
+    L.ref_free_alignment_2D_filter_references.restype = None
     # additions
     L.gpuisac_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.gpuisac_last_error.restype = ctypes.c_int
@@ -137,6 +146,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_assign_groups_device.restype = ci
     L.gpuisac_assign_groups.argtypes = [vp, cu, cu, vp]
     L.gpuisac_assign_groups.restype = ci
+    L.gpuisac_ref_free_averages.argtypes = [vp]
+    L.gpuisac_ref_free_averages.restype = ci
     L.gpuisac_nn_bias_act.argtypes = [vp, vp, cl, ci, ci, vp]
     L.gpuisac_nn_relu_backward.argtypes = [vp, vp, cl, vp]
     L.gpuisac_nn_colsum.argtypes = [vp, cl, ci, vp, ci, vp]

@@ -102,9 +102,15 @@ void pre_align_fetch(const float **img_data, unsigned int img_num, const char *b
  * clamped to +-(img_dim - ring_num - 2), angle, mirror. */
 void pre_align_run(int start_idx, int stop_idx);
 
-/* ---- adjacent paths bound by the callers (present so that ctypes binding
- * succeeds; not built in this library: each records an error and returns a
- * failure value) ---- */
+/* ---- the multigroup alignment of the stability test (aln_type
+ * "multigroup_aln"), as bin/sp_isac_applications.py:4552-4650 drives it:
+ * init with every particle's class (sorted runs 0 .. ref_num-1) and the
+ * initial class averages; the caller may write AlignParam shift_x/y; each
+ * ref_free_alignment_2D aligns every particle to its class average over the
+ * shift grid around its accumulated shift (the pre-alignment's peak and update
+ * rules), then replaces the averages by the averages of the particles
+ * transformed by their new parameters; _filter_references low-passes the
+ * averages (hyperbolic tangent); gpu_clear ends the session. ---- */
 
 /* Replaces ref_free_alignment_2D_init, cuda/gpu_aln_noref.h:101-107. */
 AlignParam *ref_free_alignment_2D_init(const AlignConfig *aln_cfg, const float **sbj_data_list,
@@ -117,6 +123,11 @@ bool ref_free_alignment_2D_size_check(const AlignConfig *cfg, unsigned int cuda_
 void ref_free_alignment_2D(void);
 /* Replaces ref_free_alignment_2D_filter_references, cuda/gpu_aln_noref.h:118. */
 void ref_free_alignment_2D_filter_references(float cutoff_freq, float falloff);
+/* No counterpart in the reference (its extract_gpu_averages,
+ * cuda/gpu_aln_noref.cu:50-81, is compiled out).  Copies the current class
+ * averages of the multigroup session, [ref_num][img_dim][img_dim], into the
+ * host array out.  Returns 0 or an error code. */
+int gpuisac_ref_free_averages(float *out);
 
 /* ---- additions of this library (no counterpart in the reference, which
  * prints and exits on any CUDA error, cuda/gpu_aln_common.cu:104-118) ---- */

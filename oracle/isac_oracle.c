@@ -265,3 +265,64 @@ static void orc_f32_peak_search(const float *ccf, unsigned n_shift, unsigned L,
 #include "isac_oracle_core.h"
 #undef P
 #undef REAL
+
+/* Reference: cu_transform_batch (cuda/gpu_aln_noref.cu:1539-1590) followed by
+ * cu_average_batch (:1592-1622), as ref_free_alignment_2D runs them
+ * (:964-996): every particle of the stack (one batch of n images in textures
+ * of tex images) is resampled through the texture at
+ *   x' = (mirror ? D - x : x) - D/2,  y' = y - D/2,
+ *   (xr, yr) = (x' cos a - y' sin a, x' sin a + y' cos a) + D/2,
+ *   sample at (xr + shift_x + 0.5, slot*D + yr + shift_y + 0.5)
+ * (each step rounded to float, the +0.5 added in double; a = DEG2RAD * angle
+ * in float, its cosine and sine computed in double and rounded to float), and
+ * class k's average is the float sum of its members' pixels in member order
+ * divided by the member count.  params[i] = (angle, shift_x, shift_y) and
+ * mirror[i]; cid_idx[n_class + 1] holds the class ranges.  Coordinates beyond
+ * +-1e6 are clamped (they read the clamped edge either way). */
+int orc_multigroup_averages(const float *stack, unsigned n, unsigned dim, unsigned tex, const float *params,
+                            const int *mirror, const unsigned *cid_idx, unsigned n_class, float *avg_out)
+{
+    if (!stack || !params || !mirror || !cid_idx || !avg_out || n == 0 || dim == 0 || tex == 0)
+        return -1;
+    orc_texture_stack ts;
+    ts.stack = stack;
+    ts.n_imgs = n;
+    ts.dim = dim;
+    ts.batch = n;
+    ts.tex = tex;
+    const float ctr = (float)(dim / 2u);
+    const float deg2rad = 3.141592653589793f / 180.0f;
+    for (unsigned k = 0; k < n_class; k++) {
+        const unsigned i0 = cid_idx[k], i1 = cid_idx[k + 1];
+        if (i1 <= i0 || i1 > n)
+            return -1;
+        for (unsigned y = 0; y < dim; y++)
+            for (unsigned x = 0; x < dim; x++) {
+                float sum = 0.0f;
+                for (unsigned i = i0; i < i1; i++) {
+                    const float rad = deg2rad * params[3 * i + 0];
+                    const float c = (float)cos((double)rad), s = (float)sin((double)rad);
+                    const float sxp = mirror[i] ? (float)(dim - x) : (float)x;
+                    const float x0 = sxp - ctr, y0 = (float)y - ctr;
+                    const float p0 = x0 * c, p1 = y0 * s, p2 = x0 * s, p3 = y0 * c;
+                    float xr = p0 - p1, yr = p2 + p3;
+                    xr = xr + ctr;
+                    yr = yr + ctr;
+                    float xs = (float)((double)(xr + params[3 * i + 1]) + 0.5);
+                    float ys = (float)((double)(yr + params[3 * i + 2]) + 0.5);
+                    xs = xs < -1.0e6f ? -1.0e6f : (xs > 1.0e6f ? 1.0e6f : xs);
+                    ys = ys < -1.0e6f ? -1.0e6f : (ys > 1.0e6f ? 1.0e6f : ys);
+                    const float yt = (float)(tex_local_index(&ts, i) * dim) + ys;
+                    int ix, iy, w[4];
+                    orc_tex_weights(xs, yt, &ix, &iy, w);
+                    const float t00 = texel(&ts, i, iy, ix), t10 = texel(&ts, i, iy, ix + 1);
+                    const float t01 = texel(&ts, i, iy + 1, ix), t11 = texel(&ts, i, iy + 1, ix + 1);
+                    const float v = ((float)w[0] * t00 + (float)w[1] * t10 + (float)w[2] * t01 +
+                                     (float)w[3] * t11) * (1.0f / 256.0f);
+                    sum = sum + v;
+                }
+                avg_out[((size_t)k * dim + y) * dim + x] = sum / (float)(i1 - i0);
+            }
+    }
+    return 0;
+}

@@ -113,6 +113,11 @@ ORC_DECLARE(f32, float)
 void orc_f64_peak_search(const double *ccf, unsigned n_shift, unsigned ring_len,
                          float *out4, double *peak, unsigned *tau);
 
+/* The multigroup alignment's class averages of transformed particles
+ * (cu_transform_batch + cu_average_batch); see isac_oracle.c. */
+int orc_multigroup_averages(const float *stack, unsigned n, unsigned dim, unsigned tex, const float *params,
+                            const int *mirror, const unsigned *cid_idx, unsigned n_class, float *avg_out);
+
 #ifdef __cplusplus
 }
 #endif

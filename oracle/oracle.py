@@ -73,6 +73,10 @@ def lib():
             f.argtypes = [cfgp, layp, fp, fp, fp, fp, rp, ctypes.c_uint, ctypes.c_int]
         L.orc_f64_peak_search.argtypes = [dp, ctypes.c_uint, ctypes.c_uint, fp, dp,
                                           ctypes.POINTER(ctypes.c_uint)]
+        L.orc_multigroup_averages.argtypes = [fp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, fp,
+                                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint),
+                                              ctypes.c_uint, fp]
+        L.orc_multigroup_averages.restype = ctypes.c_int
         L.orc_assign_groups.argtypes = [fp, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(ctypes.c_int)]
         L.orc_assign_groups.restype = ctypes.c_int
         _lib = L
@@ -277,3 +281,60 @@ def belongsto_from_id_list(id_list_long, numref: int, nima: int) -> np.ndarray:
         for i in sorted(groups[k]):
             belongsto[i] = k
     return belongsto
+
+
+def class_ranges(cid_list) -> np.ndarray:
+    """Class index ranges of sorted class runs 0..R-1 (the reference's
+    u_cid_idx, cuda/gpu_aln_noref.cu:833-843)."""
+    cid = np.asarray(cid_list, np.int64)
+    R = int(cid[-1]) + 1
+    idx = np.searchsorted(cid, np.arange(R + 1), side="left").astype(np.uint32)
+    idx[R] = cid.size
+    return idx
+
+
+def multigroup_averages(stack, params, mirror, cid_list, tex: int) -> np.ndarray:
+    """Class averages of the particles transformed by (angle, shift_x,
+    shift_y, mirror) -- cu_transform_batch + cu_average_batch restated
+    (isac_oracle.c orc_multigroup_averages).  tex: images per texture."""
+    st = np.ascontiguousarray(stack, np.float32)
+    n, D = st.shape[0], st.shape[1]
+    prm = np.ascontiguousarray(np.asarray(params, np.float32).reshape(n, 3))
+    mir = np.ascontiguousarray(np.asarray(mirror).astype(np.int32).reshape(n))
+    idx = class_ranges(cid_list)
+    R = idx.size - 1
+    out = np.zeros((R, D, D), np.float32)
+    rc = lib().orc_multigroup_averages(_fp(st), n, D, tex, _fp(prm), mir.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                       idx.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), R, _fp(out))
+    if rc:
+        raise ValueError("oracle multigroup_averages rejected its input")
+    return out
+
+
+def tanl_filter_averages(avg, cutoff: float, falloff: float) -> np.ndarray:
+    """The averages low-passed as BatchHandler::apply_tangent_filter does it
+    (cuda/gpu_aln_noref.cu:2203-2266, cu_apply_tanl_filter_to_tex :1007-1037),
+    in FP64 with numpy's real FFT: factor 0.5 (tanh(c (d + fc)) - tanh(c (d -
+    fc))) on the half spectrum, c = pi / (2 falloff fc), d = |(x, y)| with
+    x = kx / (D/2 + 1) / 2 and y = min(ky, D - ky) / (D/2) / 2, computed in
+    float as the kernel does; then the reference's host rescaling, which
+    reaches only the first image: image 0 divided by D^2, the others
+    multiplied by D^2."""
+    a = np.asarray(avg, np.float64)
+    R, D = a.shape[0], a.shape[1]
+    H = D // 2 + 1
+    f32 = np.float32
+    c = f32(f32(3.141592653589793) / (f32(2.0) * f32(falloff) * f32(cutoff)))
+    fx = (np.arange(H).astype(f32) / f32(H)) * f32(0.5)
+    half = f32(D) / f32(2.0)
+    ky = np.arange(D)
+    fy = np.where(ky.astype(f32) < half, ky, D - ky).astype(f32)
+    fy = (fy / half) * f32(0.5)
+    d = np.sqrt(fx[None, :] * fx[None, :] + fy[:, None] * fy[:, None]).astype(f32)
+    fc = f32(cutoff)
+    h = f32(0.5) * (np.tanh(c * (d + fc)) - np.tanh(c * (d - fc)))
+    out = np.fft.irfft2(np.fft.rfft2(a) * h.astype(np.float64)[None], s=(D, D))
+    n = float(D * D)
+    out[0] /= n
+    out[1:] *= n
+    return out

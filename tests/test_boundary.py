@@ -101,14 +101,36 @@ def test_align_before_init_is_an_error(lib):
     lib.gpuisac_clear_error()
 
 
-def test_adjacent_paths_fail_loudly(lib):
+def test_multigroup_before_init_fails(lib):
     from gpuisac import _lib
+    lib.gpu_clear()
     lib.gpuisac_clear_error()
-    lib.ref_free_alignment_2D.argtypes = []
-    lib.ref_free_alignment_2D.restype = None
     lib.ref_free_alignment_2D()
     code, msg = _lib.last_error(lib)
-    assert code == 4 and "multi-reference" in msg
+    assert code == 3 and "before ref_free_alignment_2D_init" in msg
+    lib.gpuisac_clear_error()
+    lib.ref_free_alignment_2D_filter_references(ctypes.c_float(0.3), ctypes.c_float(0.2))
+    assert _lib.last_error(lib)[0] == 3
+    lib.gpuisac_clear_error()
+    assert lib.gpuisac_ref_free_averages(None) == 3
+    lib.gpuisac_clear_error()
+
+
+def test_multigroup_init_rejects_bad_class_lists(lib):
+    """Classes must be sorted runs 0 .. ref_num-1 (the reference's class
+    index, cuda/gpu_aln_noref.cu:833-843); rejected before any device work."""
+    from gpuisac import _lib
+    import numpy as np
+    from gpuisac.align import make_config, ptr_array
+    imgs = np.zeros((4, 16, 16), np.float32)
+    refs = np.zeros((2, 16, 16), np.float32)
+    for cids in ([1, 1, 0, 0], [0, 0, 2, 2], [0, 1, 0, 1]):
+        cfg = make_config(4, 2, 16, 5, 256, 1.0, 1.0, 1.0, b"multigroup_aln")
+        lib.gpuisac_clear_error()
+        p = lib.ref_free_alignment_2D_init(ctypes.byref(cfg), ptr_array(imgs), ptr_array(refs),
+                                           (ctypes.c_int * 4)(*cids), 0)
+        assert not p
+        assert _lib.last_error(lib)[0] == 2
     lib.gpuisac_clear_error()
 
 
