@@ -437,6 +437,106 @@ def bench_assign(args, dev, L, d_dev, cpu=True):
     return blk
 
 
+MULTIGROUP = {"workload": "stability-test multigroup alignment: the 50,000 particles (76^2) sorted into classes of "
+                          "at most 100 (each true class split into runs), 35 rings, shift range 1 (9 shifts), "
+                          "30 iterations with the tangent filter ramp 0.1 -> 0.3, fall-off 0.2 (ISAC's defaults "
+                          "maxit=30, FH=0.3, FF=0.2)",
+              "class_size": 100, "rings": 35, "shift_range": 1.0, "iterations": 30, "cutoff": 0.3, "falloff": 0.2}
+
+
+def bench_multigroup(args, dev, L, st):
+    """One multigroup_refinement call (ref_free_alignment_2D_init, 30 x
+    (_filter_references + ref_free_alignment_2D), gpu_clear) as ISAC's
+    stability test makes it per repeat; value = particle alignments (one
+    particle against its class average over the shift grid, with the
+    averaging) per second over the iterations, e2e including the init's
+    upload of the particles and averages.  CPU baseline: one oracle iteration
+    (FP32 alignment with OpenMP, transform + average, filter) on 20 classes."""
+    import torch
+
+    from gpuisac import _lib
+    from gpuisac._lib import AlignParam
+    from gpuisac.align import make_config, ptr_array
+    from gpuisac import synth
+    m = MULTIGROUP
+    order, cid = synth.stability_classes(st.cls, m["class_size"])
+    parts = np.ascontiguousarray(st.particles[order])
+    P, D = parts.shape[0], parts.shape[1]
+    R = int(cid[-1]) + 1
+    starts = np.flatnonzero(np.r_[True, cid[1:] != cid[:-1]])
+    counts = np.diff(np.r_[starts, P])
+    avgs = np.ascontiguousarray((np.add.reduceat(parts.astype(np.float64), starts, axis=0) /
+                                 counts[:, None, None]).astype(np.float32))
+    NR, sr, n_it = m["rings"], float(m["shift_range"]), m["iterations"]
+    cfg = make_config(P, R, D, NR, 256, 1.0, sr, sr, b"multigroup_aln")
+    cids = (ctypes.c_int * P)(*[int(c) for c in cid])
+    sp, rp = ptr_array(parts), ptr_array(avgs)
+
+    def call():
+        t0 = time.perf_counter()
+        addr = L.ref_free_alignment_2D_init(ctypes.byref(cfg), sp, rp, cids, torch.cuda.current_device())
+        if not addr:
+            _lib_check(L)
+        t_init = time.perf_counter() - t0
+        prm = ctypes.cast(addr, ctypes.POINTER(AlignParam))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(n_it):
+            L.ref_free_alignment_2D_filter_references(ctypes.c_float(0.1 + (m["cutoff"] - 0.1) * i / (n_it - 1)),
+                                                      ctypes.c_float(m["falloff"]))
+            L.ref_free_alignment_2D()
+        e1.record()
+        torch.cuda.synchronize()
+        _lib.check(L)
+        # the results are in the host AlignParam array when the last call returns
+        t_all = time.perf_counter() - t0
+        assert prm[P - 1].ref_id == int(cid[-1])
+        L.gpu_clear()
+        return e0.elapsed_time(e1), t_all, t_init
+
+    for _ in range(max(1, args.warmup - 2)):
+        call()
+    launches0 = L.gpuisac_launch_count()
+    runs = [call() for _ in range(max(2, min(args.steps, 3)))]
+    launches = (L.gpuisac_launch_count() - launches0) / len(runs)
+    ms = statistics.mean(r[0] for r in runs)
+    e2e_s = statistics.mean(r[1] for r in runs)
+    blk = {"workload": m["workload"], "classes": R, "particles": P,
+           "value": P * n_it / (ms / 1000.0), "unit": "particle alignments/s",
+           "ms_per_call": ms, "ms_per_iteration": ms / n_it, "calls": len(runs),
+           "kernel_launches_per_call": launches,
+           "e2e": {"value": P * n_it / e2e_s, "unit": "particle alignments/s", "ms_per_call": 1000.0 * e2e_s,
+                   "init_ms": 1000.0 * statistics.mean(r[2] for r in runs),
+                   "h2d_bytes_per_call": int((P + R) * D * D * 4), "api": "ref_free_alignment_2D_* (host images)"}}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        n_cls = 20
+        sub = [(int(starts[j]), int(counts[j])) for j in range(n_cls)]
+        t0 = time.perf_counter()
+        filt = oracle.tanl_filter_averages(avgs[:n_cls], 0.2, m["falloff"]).astype(np.float32)
+        n_parts = 0
+        prms, mirs, sub_parts, sub_cid = [], [], [], []
+        for j, (a, n) in enumerate(sub):
+            ccfg = oracle.make_cfg(n, 1, D, NR, 256, 1.0, sr, sr)
+            lay = oracle.reference_layout(ccfg)
+            pk, _ = oracle.multi_ref_align(ccfg, lay, parts[a:a + n], filt[j:j + 1], precision="f32")
+            pk = np.asarray(pk).reshape(n, 4)
+            prms.append(pk[:, :3])
+            mirs.append(pk[:, 3] != 0)
+            sub_parts.append(parts[a:a + n])
+            sub_cid += [j] * n
+            n_parts += n
+        oracle.multigroup_averages(np.concatenate(sub_parts), np.concatenate(prms), np.concatenate(mirs), sub_cid,
+                                   65000 // D)
+        t_cpu = time.perf_counter() - t0
+        blk["cpu_baseline"] = {"value": n_parts / t_cpu, "unit": "particle alignments/s", "cores": cpu_threads(),
+                               "kind": "port",
+                               "sample": f"one iteration on {n_cls} classes ({n_parts} particles): filter, FP32 "
+                                         f"alignment (OpenMP), transform + average, {t_cpu:.1f} s"}
+    return blk
+
+
 def _lib_check(L):
     from gpuisac import _lib
     _lib.check(L)
@@ -638,6 +738,9 @@ def bench_ours(args):
         big[cls, torch.arange(100000, device=dev)] += 0.3 * torch.rand(100000, generator=rng, device=dev)
         assign_blk["synthetic_100000x500"] = bench_assign(args, dev, L, big, cpu=False)
         del big
+    multigroup_blk = None
+    if rank == 0 and world == 1 and not args.no_multigroup and WORKLOAD["workload"].startswith("mref"):
+        multigroup_blk = bench_multigroup(args, dev, L, st)
     if rank == 0 and world == 1 and not args.no_grouped:
         del d_out, peak_out
         torch.cuda.empty_cache()
@@ -657,7 +760,7 @@ def bench_ours(args):
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk,
-                "assign_groups": assign_blk}
+                "assign_groups": assign_blk, "multigroup": multigroup_blk}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -682,6 +785,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-search comparison")
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped-launch comparison")
     ap.add_argument("--no-assign", action="store_true", help="skip the group-assignment block")
+    ap.add_argument("--no-multigroup", action="store_true", help="skip the multigroup (stability test) block")
     ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])

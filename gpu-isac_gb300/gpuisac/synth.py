@@ -136,3 +136,20 @@ def workload_stack(idx: int, n_particles: int | None = None, n_refs: int | None 
     ps = None if split is None else SEED_BASE + 1000 * split + idx
     return make_stack(n_particles or w.n_particles, w.img_dim, n_refs or w.n_classes,
                       w.shift_rng, w.snr, w.blob_radius, SEED_BASE + idx, particle_seed=ps)
+
+
+def stability_classes(cls, class_size: int = 100):
+    """Particle order and class ids for a stability-test run: particles sorted
+    by class (stable), each class split into runs of at most class_size
+    (ISAC's classes hold at most img_per_grp members).  Returns (order, cid)
+    with cid the sorted runs 0..R-1."""
+    order = np.argsort(np.asarray(cls), kind="stable")
+    c = np.asarray(cls)[order]
+    cid = np.zeros(c.size, np.int64)
+    k, run, prev = -1, 0, None
+    for i, v in enumerate(c):
+        if v != prev or run == class_size:
+            k, run, prev = k + 1, 0, v
+        cid[i] = k
+        run += 1
+    return order, cid

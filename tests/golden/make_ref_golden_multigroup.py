@@ -51,7 +51,7 @@ def class_inputs(P, R, D, seed, start):
     return parts, cls, avgs, shifts
 
 
-def run_reference(lib, parts, cls, avgs, shifts, ring_num, rng, n_iter, cutoff, falloff):
+def run_reference(lib, parts, cls, avgs, shifts, ring_num, rng, n_iter, cutoff, falloff, record=True):
     fp = ctypes.POINTER(ctypes.c_float)
     lib.ref_free_alignment_2D_init.argtypes = [ctypes.POINTER(base.AlignConfig), ctypes.POINTER(fp),
                                                ctypes.POINTER(fp), ctypes.POINTER(ctypes.c_int), ctypes.c_int]
@@ -76,9 +76,39 @@ def run_reference(lib, parts, cls, avgs, shifts, ring_num, rng, n_iter, cutoff, 
             freq = 0.1 + (cutoff - 0.1) * it / float(n_iter - 1)
             lib.ref_free_alignment_2D_filter_references(freq, falloff)
         lib.ref_free_alignment_2D()
-        out.append([[prm[i].shift_x, prm[i].shift_y, prm[i].angle, float(prm[i].mirror)] for i in range(P)])
+        if record:
+            out.append([[prm[i].shift_x, prm[i].shift_y, prm[i].angle, float(prm[i].mirror)] for i in range(P)])
     lib.gpu_clear()
     return np.array(out, np.float32)
+
+
+def time_stability_workload(lib, out_dir):
+    """The reference's run time on bench.py's multigroup workload: the
+    50,000 particles of the multi-reference workload sorted into classes of
+    at most 100, class means as averages, 35 rings, shift range 1, 30
+    iterations with the filter ramp 0.1 -> 0.3, fall-off 0.2."""
+    import json
+    import sys
+    import time
+    sys.path.insert(0, os.path.join(HERE, "..", "..", "gpu-isac_gb300"))
+    from gpuisac import synth
+    st = synth.workload_stack(1)
+    order, cid = synth.stability_classes(st.cls, 100)
+    parts = np.ascontiguousarray(st.particles[order])
+    starts = np.flatnonzero(np.r_[True, cid[1:] != cid[:-1]])
+    counts = np.diff(np.r_[starts, parts.shape[0]])
+    avgs = np.ascontiguousarray((np.add.reduceat(parts.astype(np.float64), starts, axis=0) /
+                                 counts[:, None, None]).astype(np.float32))
+    times = []
+    for _ in range(2):
+        t = time.perf_counter()
+        run_reference(lib, parts, cid, avgs, None, 35, 1.0, 30, 0.3, 0.2, record=False)
+        times.append(time.perf_counter() - t)
+    res = {"workload": "multigroup_50000x76_600classes_30it", "seconds_per_call": times,
+           "particle_alignments_per_s": parts.shape[0] * 30 / min(times)}
+    with open(os.path.join(out_dir, "ref_gpu_time_multigroup.json"), "w") as f:
+        json.dump(res, f)
+    print(json.dumps(res), flush=True)
 
 
 def main():
@@ -86,8 +116,12 @@ def main():
     ap.add_argument("--ref-src", required=True)
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--build-dir", default=os.path.join(HERE, "..", "_build", "ref"))
+    ap.add_argument("--time", action="store_true", help="only time bench.py's multigroup workload")
     a = ap.parse_args()
     lib = ctypes.CDLL(base.build_ref(a.ref_src, a.build_dir))
+    if a.time:
+        time_stability_workload(lib, a.out)
+        return
     for name, P, R, D, NR, rng, n_iter, cutoff, falloff, start, seed in CASES:
         parts, cls, avgs, shifts = class_inputs(P, R, D, seed, start)
         params = run_reference(lib, parts, cls, avgs, shifts, NR, rng, n_iter, cutoff, falloff)
