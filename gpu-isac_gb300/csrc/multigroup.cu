@@ -547,7 +547,7 @@ AlignParam* ref_free_alignment_2D_init(const AlignConfig* aln_cfg, const float**
         return nullptr;
     }
     // classes are contiguous runs 0, 1, .., ref_num - 1 of the particle list
-    // (the reference builds its class index from the runs, noref.cu:833-843)
+    // (the reference builds its class index from the runs, noref.cu:825-835)
     std::vector<unsigned> cid_idx(geo.R + 1, 0);
     if (sbj_cid_list[0] != 0) {
         fail(E_ARG, "ref_free_alignment_2D_init: the class list must start with class 0");

@@ -285,7 +285,7 @@ def belongsto_from_id_list(id_list_long, numref: int, nima: int) -> np.ndarray:
 
 def class_ranges(cid_list) -> np.ndarray:
     """Class index ranges of sorted class runs 0..R-1 (the reference's
-    u_cid_idx, cuda/gpu_aln_noref.cu:833-843)."""
+    u_cid_idx, cuda/gpu_aln_noref.cu:825-835)."""
     cid = np.asarray(cid_list, np.int64)
     R = int(cid[-1]) + 1
     idx = np.searchsorted(cid, np.arange(R + 1), side="left").astype(np.uint32)

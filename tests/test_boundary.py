@@ -118,7 +118,7 @@ def test_multigroup_before_init_fails(lib):
 
 def test_multigroup_init_rejects_bad_class_lists(lib):
     """Classes must be sorted runs 0 .. ref_num-1 (the reference's class
-    index, cuda/gpu_aln_noref.cu:833-843); rejected before any device work."""
+    index, cuda/gpu_aln_noref.cu:825-835); rejected before any device work."""
     from gpuisac import _lib
     import numpy as np
     from gpuisac.align import make_config, ptr_array
