@@ -223,15 +223,17 @@ __device__ __forceinline__ float tex_sample(const StackDesc& s, const TexPlaceme
 }
 
 // Reference: polar grid centre, cuda/gpu_aln_noref.cu:1262-1269 (D/2 + shift in
-// unsigned arithmetic, base shift added in float, +0.5 in double, stored float)
+// unsigned arithmetic, base shift added in float, +0.5 in double, stored
+// float).  A float plus 0.5 is exact in double, so rounding that sum to float
+// is the float addition itself: half_up(f) == (float)((double)f + 0.5).
+__device__ __forceinline__ float half_up(float f) { return __fadd_rn(f, 0.5f); }
+
 __device__ __forceinline__ float centre_coord(unsigned dim, int shift, const float* base)
 {
     unsigned u = dim / 2u + (unsigned)shift;
-    if (base) {
-        float f = (float)u + *base;
-        return (float)((double)f + 0.5);
-    }
-    return (float)((double)u + 0.5);
+    if (base)
+        return half_up(__fadd_rn((float)u, *base));
+    return half_up((float)u); // u < 2^24: exact as float
 }
 
 } // namespace gpuisac

@@ -80,8 +80,8 @@ mg_average_kernel(StackDesc st, const MgXform* __restrict__ xf, const unsigned* 
         float yr = __fadd_rn(__fmul_rn(x0, t.s), __fmul_rn(y0, t.c));
         xr = __fadd_rn(xr, ctr);
         yr = __fadd_rn(yr, ctr);
-        float xs = (float)((double)__fadd_rn(xr, t.sx) + 0.5);
-        float ys = (float)((double)__fadd_rn(yr, t.sy) + 0.5);
+        float xs = half_up(__fadd_rn(xr, t.sx));
+        float ys = half_up(__fadd_rn(yr, t.sy));
         // far-outside coordinates read the clamped edge either way; keep the
         // fixed-point conversion in range
         xs = fminf(fmaxf(xs, -1.0e6f), 1.0e6f);

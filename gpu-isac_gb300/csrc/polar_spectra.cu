@@ -58,7 +58,8 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
     const float yoff = (float)(place.local * st.dim);
 
     // thread tid samples angle tid of every ring; FP32 ring-weighted partial
-    // sums feed the FP64 image mean / deviation
+    // sums, reduced in FP32 across each warp, feed the image mean / deviation
+    // (the eight warp sums are added in FP64)
     float s1 = 0.f, s2 = 0.f;
 #pragma unroll 4
     for (unsigned r = 0; r < ring_num; r++) {
@@ -71,12 +72,12 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
         s1 += w * v;
         s2 += w * v * v;
     }
-    double d1 = s1, d2 = s2;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        d1 += __shfl_xor_sync(0xffffffffu, d1, off);
-        d2 += __shfl_xor_sync(0xffffffffu, d2, off);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, off);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, off);
     }
+    const double d1 = s1, d2 = s2;
     const int warp = tid >> 5, lane = tid & 31;
     if (lane == 0) {
         red[warp] = d1;
