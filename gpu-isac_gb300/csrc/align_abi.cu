@@ -216,9 +216,12 @@ struct Workspace {
     DevBuf<float2> tmpl, tw, shifts_f, ref_sp, sbj_sp, base;
     DevBuf<int2> shifts_i, zero_shift;
     DevBuf<unsigned> err; // device-side timeout flag of the kernels' bounded waits
+    TexStack ref_tex, sbj_tex; // the stacks as textures for the texture unit
     void release()
     {
         err.release();
+        ref_tex.release();
+        sbj_tex.release();
         geo_D = geo_NR = 0;
         geo_shifts.clear();
         zero_shift.release();
@@ -353,9 +356,17 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
     const size_t row_elems = (size_t)g.NR * kSlots; // float2 per (image, shift) row
     if (ws.ref_sp.ensure(row_elems * std::max(g.R, 1u)))
         return E_NOMEM;
+    // both stacks as the reference's textures, sampled by the texture unit
+    const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
+    if (texture_unit_enabled()) {
+        CK(ws.ref_tex.build(refs, st));
+        CK(ws.sbj_tex.build(sbjs, st));
+        ref_tx = ws.ref_tex.objects();
+        sbj_tx = ws.sbj_tex.objects();
+    }
     cudaEvent_t ev = g_timer.begin(st);
     CK(launch_polar_spectra(refs, ws.tmpl.p, ws.tw.p, g.NR, ws.zero_shift.p, 1, nullptr, 0,
-                            g.R, 1, ws.ref_sp.p, st));
+                            g.R, 1, ws.ref_sp.p, st, nullptr, ref_tx));
     g_timer.end(K_SPECTRA, ev, st);
 
     // particle chunk: bounded by the requested share of free memory
@@ -375,7 +386,7 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
         unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
         ev = g_timer.begin(st);
         CK(launch_polar_spectra(sbjs, ws.tmpl.p, ws.tw.p, g.NR, ws.shifts_i.p, g.S, d_base, p0, n, 0, ws.sbj_sp.p,
-                                st));
+                                st, nullptr, sbj_tx));
         g_timer.end(K_SPECTRA, ev, st);
         ev = g_timer.begin(st);
         CK(launch_ccf_peak(ws.sbj_sp.p, ws.ref_sp.p, ws.tw.p, g.NR, g.S, g.R, n, p0, g.P, ws.shifts_f.p, d_base, d_out,
@@ -766,9 +777,14 @@ int gpuisac_spectra_device_layout(const AlignConfig* cfg, const float* imgs, uns
     if (rc)
         return rc;
     StackDesc sd{imgs, n_img, g.D, std::min(batch, std::max(n_img, 1u)), tex};
+    const unsigned long long* tx = nullptr;
+    if (texture_unit_enabled() && n_img > 0) {
+        CK(ws.sbj_tex.build(sd, st));
+        tx = ws.sbj_tex.objects();
+    }
     CK(launch_polar_spectra(sd, ws.tmpl.p, ws.tw.p, g.NR, is_ref ? ws.zero_shift.p : ws.shifts_i.p, is_ref ? 1 : g.S,
                             reinterpret_cast<const float2*>(base_shift), 0, n_img, is_ref,
-                            reinterpret_cast<float2*>(out), st));
+                            reinterpret_cast<float2*>(out), st, nullptr, tx));
     CK(cudaStreamSynchronize(st));
     return 0;
 }

@@ -128,6 +128,7 @@ struct StackDesc {
 
 struct TexPlacement {
     unsigned local;      // image index inside its texture (the reference's block index)
+    unsigned tex_id;     // texture (batch-major, textures of a batch in order) holding the image
     unsigned tex_first;  // global index of the texture's slot 0
     unsigned batch_end;  // one past the last image of the current batch
     long rows;           // texture height in rows
@@ -143,6 +144,7 @@ __device__ __forceinline__ TexPlacement tex_place(const StackDesc& s, unsigned i
     unsigned n_tex_alloc = (s.batch + s.tex - 1) / s.tex;
     unsigned alloc = (tex_idx != n_tex_alloc - 1) ? s.tex : s.batch - tex_idx * s.tex;
     t.local = loc - tex_idx * s.tex;
+    t.tex_id = (bstart / s.batch) * n_tex_alloc + tex_idx;
     t.tex_first = bstart + tex_idx * s.tex;
     t.batch_end = bstart + blen;
     t.rows = (long)alloc * s.dim;

@@ -5,6 +5,7 @@
 #include <stddef.h>
 
 #include <atomic>
+#include <vector>
 
 #include "gpuisac_device.cuh"
 
@@ -31,14 +32,43 @@ size_t ccf_peak_smem_bytes(unsigned ring_num);
 // kernels launched by this library since load (all launchers count here)
 extern std::atomic<unsigned long long> g_kernel_launches;
 
+// A device stack laid out as the reference's textures hold it (batches of
+// st.batch images in textures of st.tex images, stale slots of a short final
+// batch filled from the previous batch), one texture object per segment
+// (tex_stack.cu).  prepare() allocates the layout and creates the objects
+// (kept while the geometry stays the same; not inside a stream capture);
+// fill() copies st.img into every slot on `stream` (a kernel, capturable);
+// build() is both.
+struct TexStack {
+    unsigned char* mem = nullptr;
+    size_t mem_bytes = 0, pitch_ = 0, full_bytes_ = 0, batch_bytes_ = 0;
+    std::vector<unsigned long long> objs;
+    unsigned long long* d_objs = nullptr;
+    size_t d_objs_n = 0;
+    unsigned n = 0, dim = 0, batch = 0, tex = 0, n_batches = 0;
+    int device = -1;
+    cudaError_t prepare(const StackDesc& st);
+    cudaError_t fill(const StackDesc& st, cudaStream_t stream);
+    cudaError_t build(const StackDesc& st, cudaStream_t stream);
+    const unsigned long long* objects() const { return d_objs; }
+    void destroy_objects();
+    void release();
+};
+
+// Whether the kernels sample through the texture unit (TexStack) where the
+// caller has one: on unless the environment sets GPUISAC_TEXTURE=0.
+bool texture_unit_enabled();
+
 // Resample + normalise + ring FFT of n_img images x n_shift shifts: images
 // img0 .. img0 + n_img - 1 of the stack, or img_list[0 .. n_img-1] (device)
 // when a list is given.  out: [n_img][n_shift][ring_num][kSlots] float2
-// (see polar_spectra.cu).
+// (see polar_spectra.cu).  tex_objs: texture objects of st built by a
+// TexStack (samples through the texture unit), or null (the emulation).
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,
                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
-                                 float2* out, cudaStream_t stream, const unsigned* img_list = nullptr);
+                                 float2* out, cudaStream_t stream, const unsigned* img_list = nullptr,
+                                 const unsigned long long* tex_objs = nullptr);
 
 // CCF against every reference + inverse FFT + peak search for n_part particles
 // whose spectra are in sbj_sp ([n_part][n_shift][ring_num][kSlots]); results

@@ -89,6 +89,7 @@ struct GroupState {
     Buf<CcfGroup> table;
     Buf<unsigned> err;
     Plan plan;
+    std::vector<TexStack> ref_tex, sbj_tex; // each group's stacks as textures
     std::vector<float2> h_tw, h_tmpl, h_sf;
     std::vector<int2> h_si;
 } g_groups;
@@ -150,6 +151,8 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     append(key, &st, sizeof(st));
     const CcfTile key_tile = ccf_tile(geo.NR, geo.S, true); // another tile shape records a new graph
     append(key, &key_tile, sizeof(key_tile));
+    const bool hw = texture_unit_enabled();
+    append(key, &hw, sizeof(hw));
     if (S.plan.exec && S.plan.key == key) {
         G_CK(cudaMemsetAsync(S.err.p, 0, sizeof(unsigned), st));
         G_CK(cudaGraphLaunch(S.plan.exec, st));
@@ -168,6 +171,33 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     const int variant = tile.variant;
     const unsigned qt = ccf_refs_per_item(NR, variant);
     const unsigned ppc = tile.ppc;
+
+    // every group's stacks as the reference's textures (allocated and bound
+    // here; filled inside the recorded sequence)
+    auto ref_desc = [&](const GpuisacGroup& g) {
+        return StackDesc{ref + (size_t)g.ref_offset * D * D, g.ref_num, D, std::max(1u, std::min(g.ref_num, 100u)),
+                         tex};
+    };
+    auto sbj_desc = [&](const GpuisacGroup& g) {
+        AlignConfig gc = *cfg;
+        gc.sbj_num = g.sbj_num;
+        gc.ref_num = g.ref_num;
+        return StackDesc{sbj + (size_t)g.sbj_offset * D * D, g.sbj_num, D, reference_batch(&gc), tex};
+    };
+    for (size_t i = n_groups; i < S.ref_tex.size(); i++) {
+        S.ref_tex[i].release();
+        S.sbj_tex[i].release();
+    }
+    S.ref_tex.resize(n_groups);
+    S.sbj_tex.resize(n_groups);
+    if (hw)
+        for (unsigned gi = 0; gi < n_groups; gi++) {
+            const GpuisacGroup& g = groups[gi];
+            if (g.ref_num == 0 || g.sbj_num == 0)
+                continue;
+            G_CK(S.ref_tex[gi].prepare(ref_desc(g)));
+            G_CK(S.sbj_tex[gi].prepare(sbj_desc(g)));
+        }
 
     size_t free_b = 0, total_b = 0;
     G_CK(cudaMemGetInfo(&free_b, &total_b));
@@ -262,23 +292,28 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
         const GpuisacGroup& g = groups[gi];
         if (g.ref_num == 0 || g.sbj_num == 0)
             continue;
-        StackDesc rs{ref + (size_t)g.ref_offset * D * D, g.ref_num, D, std::max(1u, std::min(g.ref_num, 100u)), tex};
+        const StackDesc rs = ref_desc(g);
+        if (hw) {
+            e = S.ref_tex[gi].fill(rs, cap);
+            if (e == cudaSuccess)
+                e = S.sbj_tex[gi].fill(sbj_desc(g), cap);
+            if (e != cudaSuccess)
+                break;
+        }
         e = launch_polar_spectra(rs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, g.ref_num, 1,
-                                 S.ref_sp.p + ref_row[gi] * row_elems, cap);
+                                 S.ref_sp.p + ref_row[gi] * row_elems, cap, nullptr,
+                                 hw ? S.ref_tex[gi].objects() : nullptr);
     }
     for (const Wave& w : waves) {
         for (const Segment& sg : w.segs) {
             if (e != cudaSuccess)
                 break;
             const GpuisacGroup& g = groups[sg.group];
-            AlignConfig gc = *cfg;
-            gc.sbj_num = g.sbj_num;
-            gc.ref_num = g.ref_num;
-            const unsigned batch = reference_batch(&gc);
-            StackDesc ss{sbj + (size_t)g.sbj_offset * D * D, g.sbj_num, D, batch, tex};
+            const StackDesc ss = sbj_desc(g);
             const float2* bs = base_shift ? reinterpret_cast<const float2*>(base_shift) + g.sbj_offset : nullptr;
             e = launch_polar_spectra(ss, S.tmpl.p, S.tw.p, NR, S.shifts_i.p, Sn, bs, sg.a, sg.b - sg.a, 0,
-                                     S.sbj_sp.p + sg.row * row_elems * Sn, cap);
+                                     S.sbj_sp.p + sg.row * row_elems * Sn, cap, nullptr,
+                                     hw ? S.sbj_tex[sg.group].objects() : nullptr);
         }
         if (e != cudaSuccess)
             break;

@@ -61,7 +61,7 @@ struct MgXform {
 // count in float.
 __global__ void __launch_bounds__(256)
 mg_average_kernel(StackDesc st, const MgXform* __restrict__ xf, const unsigned* __restrict__ cid_idx,
-                  float* __restrict__ avg)
+                  float* __restrict__ avg, const unsigned long long* __restrict__ tex_objs)
 {
     const unsigned k = blockIdx.y;
     const unsigned D = st.dim;
@@ -87,7 +87,11 @@ mg_average_kernel(StackDesc st, const MgXform* __restrict__ xf, const unsigned* 
         xs = fminf(fmaxf(xs, -1.0e6f), 1.0e6f);
         ys = fminf(fmaxf(ys, -1.0e6f), 1.0e6f);
         const TexPlacement pl = tex_place(st, i);
-        sum = __fadd_rn(sum, tex_sample(st, pl, xs, __fadd_rn((float)(pl.local * D), ys)));
+        const float yt = __fadd_rn((float)(pl.local * D), ys);
+        // the texture unit when the stack has textures, else its emulation
+        const float v = tex_objs ? tex2D<float>((cudaTextureObject_t)__ldg(tex_objs + pl.tex_id), xs, yt)
+                                 : tex_sample(st, pl, xs, yt);
+        sum = __fadd_rn(sum, v);
     }
     avg[(size_t)k * D * D + q] = __fdiv_rn(sum, (float)(i1 - i0));
 }
@@ -234,6 +238,7 @@ struct MgState {
     DBuf<float2> tw, tmpl, shifts_f, ref_sp, sbj_sp, base, ftw, fscratch;
     DBuf<int2> shifts_i, zero;
     DBuf<float4> peak;
+    TexStack sbj_tex, ref_tex; // the particles (built at init) and the averages (each iteration)
     DBuf<unsigned> err, cid;
     DBuf<MgXform> xf;
     DBuf<CcfGroup> table;
@@ -263,6 +268,8 @@ void clear_mg(MgState& s)
     s.cid.release();
     s.xf.release();
     s.table.release();
+    s.sbj_tex.release();
+    s.ref_tex.release();
     std::free(s.params);
     s.params = nullptr;
     s.cid_idx.clear();
@@ -337,7 +344,17 @@ int run_iteration(MgState& s)
     // the class averages at zero shift (reference basis, ring weights folded
     // in), read as one texture of R images
     StackDesc refs{s.ref.p, R, D, R, s.tex};
-    MG_CK(launch_polar_spectra(refs, s.tmpl.p, s.tw.p, NR, s.zero.p, 1, nullptr, 0, R, 1, s.ref_sp.p, st));
+    StackDesc sbjs{s.sbj.p, P, D, P, s.tex};
+    const bool hw = texture_unit_enabled();
+    if (hw) {
+        MG_CK(s.ref_tex.build(refs, st));
+        if (!s.sbj_tex.objects())
+            MG_CK(s.sbj_tex.build(sbjs, st));
+    }
+    const unsigned long long* ref_tx = hw ? s.ref_tex.objects() : nullptr;
+    const unsigned long long* sbj_tx = hw ? s.sbj_tex.objects() : nullptr;
+    MG_CK(launch_polar_spectra(refs, s.tmpl.p, s.tw.p, NR, s.zero.p, 1, nullptr, 0, R, 1, s.ref_sp.p, st, nullptr,
+                               ref_tx));
 
     // base shifts: the particles' accumulated shifts
     s.h_base.resize(P);
@@ -396,10 +413,9 @@ int run_iteration(MgState& s)
     MG_CK(cudaMemcpyAsync(s.table.p, s.h_table.data(), s.h_table.size() * sizeof(CcfGroup),
                           cudaMemcpyHostToDevice, st));
 
-    StackDesc sbjs{s.sbj.p, P, D, P, s.tex};
     for (const ChunkWork& cw : work) {
         MG_CK(launch_polar_spectra(sbjs, s.tmpl.p, s.tw.p, NR, s.shifts_i.p, S, s.base.p, cw.c0, cw.c, 0, s.sbj_sp.p,
-                                   st));
+                                   st, nullptr, sbj_tx));
         CcfWork w{};
         w.groups = s.table.p + cw.first;
         w.n_groups = cw.n_groups;
@@ -434,7 +450,7 @@ int run_iteration(MgState& s)
     }
     MG_CK(cudaMemcpyAsync(s.xf.p, s.h_xf.data(), P * sizeof(MgXform), cudaMemcpyHostToDevice, st));
     dim3 grid((D * D + 255) / 256, R);
-    mg_average_kernel<<<grid, 256, 0, st>>>(sbjs, s.xf.p, s.cid.p, s.ref.p);
+    mg_average_kernel<<<grid, 256, 0, st>>>(sbjs, s.xf.p, s.cid.p, s.ref.p, sbj_tx);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     MG_CK(cudaGetLastError());
     MG_CK(cudaStreamSynchronize(st));

@@ -27,7 +27,8 @@ __global__ void __launch_bounds__(256, 4)
 polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
                      unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
                      const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
-                     float2* __restrict__ out, const unsigned* __restrict__ img_list)
+                     float2* __restrict__ out, const unsigned* __restrict__ img_list,
+                     const unsigned long long* __restrict__ tex_objs)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // ring pair p's samples at polar[p * 2 * kPairStride + (r & 1) * 256 + angle];
@@ -56,6 +57,8 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
     const float cnt_y = centre_coord(st.dim, sh.y, by);
     const TexPlacement place = tex_place(st, img);
     const float yoff = (float)(place.local * st.dim);
+    // the texture unit itself when the stack has textures, else its emulation
+    const cudaTextureObject_t tobj = tex_objs ? (cudaTextureObject_t)__ldg(tex_objs + place.tex_id) : 0;
 
     // thread tid samples angle tid of every ring; FP32 ring-weighted partial
     // sums, reduced in FP32 across each warp, feed the image mean / deviation
@@ -66,7 +69,7 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
         float2 o = __ldg(&tmpl[r * kRingLen + tid]);
         float x = cnt_x + o.x;
         float y = (yoff + cnt_y) + o.y;
-        float v = tex_sample(st, place, x, y);
+        float v = tex_objs ? tex2D<float>(tobj, x, y) : tex_sample(st, place, x, y);
         polar[polar_index(r) + tid] = v;
         float w = (float)(r + 1);
         s1 += w * v;
@@ -152,7 +155,8 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,
                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
-                                 float2* out, cudaStream_t stream, const unsigned* img_list)
+                                 float2* out, cudaStream_t stream, const unsigned* img_list,
+                                 const unsigned long long* tex_objs)
 {
     if (n_img == 0 || n_shift == 0)
         return cudaSuccess;
@@ -167,7 +171,7 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
     }
     unsigned rows = n_img * n_shift;
     polar_spectra_kernel<<<rows, 256, smem, stream>>>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base,
-                                                       img0, n_img, is_ref, out, img_list);
+                                                       img0, n_img, is_ref, out, img_list, tex_objs);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

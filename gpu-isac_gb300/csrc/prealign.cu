@@ -80,6 +80,7 @@ struct PreState {
     DBuf<float> d;
     DBuf<float4> peak;
     DBuf<unsigned> err;
+    TexStack sbj_tex;
     float* h_stage = nullptr;
     size_t h_stage_n = 0;
     std::vector<float4> h_peak;
@@ -101,6 +102,7 @@ void clear_pre(PreState& s)
     s.d.release();
     s.peak.release();
     s.err.release();
+    s.sbj_tex.release();
     if (s.h_stage)
         cudaFreeHost(s.h_stage);
     s.h_stage = nullptr;
@@ -347,10 +349,15 @@ void pre_align_run(int start_idx, int stop_idx)
             1, std::min<size_t>({(size_t)n, (size_t)(0.4 * (double)free_b) / per_part, (size_t)16384}));
         PRE_CK(s.sbj_sp.ensure(row * g.S * chunk));
         StackDesc sbjs{s.sbj.p, s.capacity, g.D, s.capacity, tex};
+        const unsigned long long* sbj_tx = nullptr;
+        if (texture_unit_enabled()) {
+            PRE_CK(s.sbj_tex.build(sbjs, st));
+            sbj_tx = s.sbj_tex.objects();
+        }
         for (unsigned c0 = 0; c0 < n; c0 += chunk) {
             const unsigned c = std::min(chunk, n - c0);
             PRE_CK(launch_polar_spectra(sbjs, s.tmpl.p, s.tw.p, g.NR, s.shifts_i.p, g.S, s.base.p, c0, c, 0,
-                                        s.sbj_sp.p, st));
+                                        s.sbj_sp.p, st, nullptr, sbj_tx));
             PRE_CK(launch_ccf_peak(s.sbj_sp.p, s.ref_sp.p, s.tw.p, g.NR, g.S, 1, c, c0, n, s.shifts_f.p, s.base.p,
                                    s.d.p, s.peak.p, s.err.p, st, kPeakPreAlign));
         }

@@ -65,6 +65,7 @@ struct PropState {
     Buf<int2> shifts_i, zero;
     Buf<CcfGroup> table;
     Buf<unsigned> err, sel;
+    TexStack ref_tex, sbj_tex;
 } g_prop;
 
 } // namespace
@@ -136,7 +137,13 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
 
     // reference spectra: every reference, stacked as the reference stacks them
     StackDesc refs{ref, geo.R, D, std::max(1u, std::min(geo.R, 100u)), tex};
-    P_CK(launch_polar_spectra(refs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, geo.R, 1, S.ref_sp.p, st));
+    const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
+    if (texture_unit_enabled()) {
+        P_CK(S.ref_tex.build(refs, st));
+        ref_tx = S.ref_tex.objects();
+    }
+    P_CK(launch_polar_spectra(refs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, geo.R, 1, S.ref_sp.p, st, nullptr,
+                              ref_tx));
 
     // one group per selected particle: 1 particle x its k references
     const unsigned tiles = (k + qt - 1) / qt;
@@ -149,6 +156,10 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
     P_CK(S.sbj_sp.ensure(row_elems * Sn * std::min(chunk, n_sel)));
     const float2* bs = reinterpret_cast<const float2*>(base_shift);
     StackDesc sbjs{sbj, geo.P, D, geo.sbj_batch, tex};
+    if (texture_unit_enabled()) {
+        P_CK(S.sbj_tex.build(sbjs, st));
+        sbj_tx = S.sbj_tex.objects();
+    }
     const unsigned* sel_dev = part_idx;
     for (unsigned c0 = 0; c0 < n_sel; c0 += chunk) {
         const unsigned n = std::min(chunk, n_sel - c0);
@@ -171,7 +182,7 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
         }
         P_CK(cudaMemcpyAsync(S.table.p + c0, table.data() + c0, n * sizeof(CcfGroup), cudaMemcpyHostToDevice, st));
         P_CK(launch_polar_spectra(sbjs, S.tmpl.p, S.tw.p, NR, S.shifts_i.p, Sn, bs, c0, n, 0, S.sbj_sp.p, st,
-                                  sel_dev ? sel_dev + c0 : nullptr));
+                                  sel_dev ? sel_dev + c0 : nullptr, sbj_tx));
         CcfWork w{};
         w.groups = S.table.p + c0;
         w.n_groups = n;
@@ -262,6 +273,7 @@ struct LearnState {
     Buf<unsigned> err, prop, fb_list, fb_flag;
     Buf<float> X, H, Z, E, nrm, G, Smax, dk, dfb;
     Buf<float4> pkk, pfb;
+    TexStack ref_tex, sbj_tex;
 } g_learn;
 
 } // namespace
@@ -315,7 +327,13 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
 
     // reference spectra for the search (reference basis, every reference)
     StackDesc refs{ref, R, D, std::max(1u, std::min(R, 100u)), tex};
-    P_CK(launch_polar_spectra(refs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, R, 1, S.ref_sp.p, st));
+    const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
+    if (texture_unit_enabled()) {
+        P_CK(S.ref_tex.build(refs, st));
+        ref_tx = S.ref_tex.objects();
+    }
+    P_CK(launch_polar_spectra(refs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, R, 1, S.ref_sp.p, st, nullptr,
+                              ref_tx));
 
     // chunk of particles: spectra at every shift, network activations over
     // every (particle, shift) row, scores, proposals and both searches
@@ -347,6 +365,10 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
 
     const float2* bs = reinterpret_cast<const float2*>(base_shift);
     StackDesc sbjs{sbj, P, D, geo.sbj_batch, tex};
+    if (texture_unit_enabled()) {
+        P_CK(S.sbj_tex.build(sbjs, st));
+        sbj_tx = S.sbj_tex.objects();
+    }
     std::vector<CcfGroup> table(chunk);
     std::vector<unsigned> flags(chunk), fbl;
     unsigned long long n_pairs = 0;
@@ -379,7 +401,8 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
         const unsigned n = std::min(chunk, P - c0);
         const long rows = (long)n * Sn;
         // 1. subject spectra at every shift
-        P_CK(launch_polar_spectra(sbjs, S.tmpl.p, S.tw.p, NR, S.shifts_i.p, Sn, bs, c0, n, 0, S.sbj_sp.p, st));
+        P_CK(launch_polar_spectra(sbjs, S.tmpl.p, S.tw.p, NR, S.shifts_i.p, Sn, bs, c0, n, 0, S.sbj_sp.p, st, nullptr,
+                                  sbj_tx));
         // 2. standardised ring features of every (particle, shift) row
         NN_CK(gpuisac_nn_features(reinterpret_cast<const float*>(S.sbj_sp.p), (unsigned)rows, NR, net->nk, net->mu,
                                   net->inv_sd, S.X.p, st));

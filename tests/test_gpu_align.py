@@ -149,3 +149,29 @@ def test_ccf_kernel_variants_agree(gpulib, cuda, oracle_mod, D, NR, monkeypatch)
         assert np.array_equal(runs[""][0], runs[sel][0]) and np.array_equal(runs[""][1], runs[sel][1]), sel
     d0, dg = runs[""][1].astype(np.float64), runs["general"][1].astype(np.float64)
     assert (np.abs(d0 - dg) / np.maximum(np.abs(dg), 1e-30)).max() <= PEAK_RTOL
+
+
+@pytest.mark.parametrize("P,D,NR,base", [(300, 64, 29, False), (160, 76, 35, True)])
+def test_texture_unit_matches_emulation(gpulib, cuda, monkeypatch, P, D, NR, base):
+    """The whole alignment sampled through the texture unit (the default) and
+    through its emulation (GPUISAC_TEXTURE=0): the same tap weights, so peak
+    values agree to 1e-5 relative and the (angle, shift, mirror) tuples on
+    >= 99.5 % of pairs."""
+    import torch
+    from gpuisac.align import multi_ref_align_device
+    st = synth.make_stack(P, D, 10, 2, 0.1, 0.37 * D, 77)
+    parts = torch.from_numpy(st.particles).to(cuda)
+    refs = torch.from_numpy(st.refs).to(cuda)
+    b = None
+    if base:
+        b = torch.from_numpy((np.round(np.random.default_rng(5).uniform(-1.5, 1.5, (P, 2)) * 64) / 64)
+                             .astype(np.float32)).to(cuda)
+    out = []
+    for flag in ("0", "1"):
+        monkeypatch.setenv("GPUISAC_TEXTURE", flag)
+        d, pk = multi_ref_align_device(parts, refs, NR, 2.0, 2.0, base_shifts=b)
+        out.append((d.cpu().numpy().astype(np.float64), pk.cpu().numpy()))
+    (d0, p0), (d1, p1) = out
+    assert (np.abs(d1 - d0) / np.maximum(np.abs(d0), 1e-30)).max() <= 1e-5
+    same = (p1[..., 1:] == p0[..., 1:]).all(-1) & (circ_diff(p1[..., 0], p0[..., 0]) < ANGLE_TOL)
+    assert same.mean() >= 0.995, same.mean()

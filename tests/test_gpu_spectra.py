@@ -119,3 +119,25 @@ def test_single_ring_and_no_shift(gpulib, cuda, oracle_mod):
     lay = oracle_mod.OrcLayout(3, gpulib.get_texture_limit(48), 1)
     gpu = decode(run_gpu(gpulib, cuda, st.particles, gcfg, False), False)
     check(gpu, oracle_spectra(oracle_mod, st.particles, ocfg, lay, False))
+
+
+@pytest.mark.parametrize("n,batch,tex", [(20, 7, 3), (33, 10, 10), (9, 9, 4)])
+def test_texture_unit_equals_emulation_on_stacked_layouts(gpulib, cuda, monkeypatch, n, batch, tex):
+    """The spectra sampled through the texture unit (TexStack: batches,
+    textures, stale slots of a short final batch) and through its emulation
+    (GPUISAC_TEXTURE=0) on layouts where edge taps read neighbouring and
+    stale images: the tap weights are the texture unit's own, so the spectra
+    agree to the blend's rounding (1e-5 of the row's largest value)."""
+    from gpuisac import make_config
+    D, NR = 32, 15      # rings reach the image edge: taps cross into neighbours
+    rng = np.random.default_rng(n * 100 + batch)
+    imgs = rng.standard_normal((n, D, D)).astype(np.float32)
+    base = (np.round(rng.uniform(-1.5, 1.5, (n, 2)) * 64) / 64).astype(np.float32)
+    cfg = make_config(n, 1, D, NR, 256, 1.0, 2.0, 2.0)
+    monkeypatch.setenv("GPUISAC_TEXTURE", "0")
+    emu = run_gpu(gpulib, cuda, imgs, cfg, False, base=base, layout=(batch, tex))
+    monkeypatch.setenv("GPUISAC_TEXTURE", "1")
+    hw = run_gpu(gpulib, cuda, imgs, cfg, False, base=base, layout=(batch, tex))
+    scale = np.abs(emu).reshape(n, -1).max(1)
+    err = np.abs(hw - emu).reshape(n, -1).max(1) / scale
+    assert err.max() <= 1e-5, err.max()
