@@ -300,7 +300,9 @@ def bench_learned(args, dev, L, spec=None):
             "train": {"particles": n_train, "seconds_incl_labelling": t_train, "loss_first_last":
                       [rep.loss[0], rep.loss[-1]], "epochs": len(rep.loss)},
             "gen_seconds": t_gen, "gpu_launches_per_step": launches,
-            "dtype": "f32 network (CUDA cores), f32 search"}
+            "dtype": ("f32 network (CUDA cores)" if os.environ.get("GPUISAC_NN_FP32", "0") not in ("", "0")
+                      else "bf16 network inference (tcgen05 tensor cores, f32 accumulate; training f32)")
+                     + ", f32 search"}
 
 
 GROUPED = dict(workload="groups_400_loguniform_100_5000_x76_10to60ref", n_groups=400, min_size=100, max_size=5000,
