@@ -721,7 +721,8 @@ def bench_ours(args):
         d2h = R * P * 4 + R * P * 16
         e2e = {"value": world * alignments / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s, "steps": args.e2e_steps,
-               "host_to_device": "pinned staging of the caller's image pointers"}
+               "host_to_device": "the caller's image memory read directly (contiguous runs of the pointer list); "
+                                 "results copied back per chunk while the next chunk computes"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

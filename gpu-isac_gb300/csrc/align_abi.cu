@@ -217,8 +217,18 @@ struct Workspace {
     DevBuf<int2> shifts_i, zero_shift;
     DevBuf<unsigned> err; // device-side timeout flag of the kernels' bounded waits
     TexStack ref_tex, sbj_tex; // the stacks as textures for the texture unit
+    cudaStream_t copy_stream = nullptr; // results to the host, overlapping the next chunk
+    cudaEvent_t chunk_done[2] = {nullptr, nullptr};
     void release()
     {
+        for (int i = 0; i < 2; i++) {
+            if (chunk_done[i])
+                cudaEventDestroy(chunk_done[i]);
+            chunk_done[i] = nullptr;
+        }
+        if (copy_stream)
+            cudaStreamDestroy(copy_stream);
+        copy_stream = nullptr;
         err.release();
         ref_tex.release();
         sbj_tex.release();
@@ -335,9 +345,20 @@ struct KernelTimer {
 enum { K_SPECTRA = 0, K_CCF = 1 };
 
 // ---------------------------------------------------------------- the pipeline
+// Host destinations of the results (the reference-facing call): d [R][pitch]
+// and peak_list [R][4P] in the caller's memory.
+struct HostOut {
+    float* d = nullptr;
+    unsigned d_pitch = 0;
+    float* peak = nullptr;
+};
+
 // Device-resident multi-reference alignment of P particles against R refs.
+// With host destinations, each chunk's columns are copied back on a second
+// stream while the next chunk computes.
 int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, const float* d_sbj, const float* d_ref,
-                  const float2* d_base, float* d_out, float4* d_peak, float mem_request, cudaStream_t st)
+                  const float2* d_base, float* d_out, float4* d_peak, float mem_request, cudaStream_t st,
+                  const HostOut* host = nullptr)
 {
     int dev = 0;
     CK(cudaGetDevice(&dev));
@@ -382,6 +403,25 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
     if (ws.err.ensure(1))
         return E_NOMEM;
     CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), st));
+    // a chunk's results to the host, on the copy stream after its kernels
+    // (event chunk_done[slot], recorded right after the chunk's CCF launch)
+    unsigned prev_p0 = 0, prev_n = 0, slot = 0;
+    auto copy_back = [&](unsigned c0, unsigned cn, unsigned ev_slot) -> int {
+        CK(cudaStreamWaitEvent(ws.copy_stream, ws.chunk_done[ev_slot], 0));
+        CK(cudaMemcpy2DAsync(host->d + c0, (size_t)host->d_pitch * sizeof(float), d_out + c0, (size_t)g.P * sizeof(float),
+                             (size_t)cn * sizeof(float), g.R, cudaMemcpyDeviceToHost, ws.copy_stream));
+        CK(cudaMemcpy2DAsync(host->peak + 4 * (size_t)c0, (size_t)g.P * sizeof(float4), d_peak + c0,
+                             (size_t)g.P * sizeof(float4), (size_t)cn * sizeof(float4), g.R, cudaMemcpyDeviceToHost,
+                             ws.copy_stream));
+        return 0;
+    };
+    if (host) {
+        if (!ws.copy_stream)
+            CK(cudaStreamCreateWithFlags(&ws.copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; i++)
+            if (!ws.chunk_done[i])
+                CK(cudaEventCreateWithFlags(&ws.chunk_done[i], cudaEventDisableTiming));
+    }
     for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk) {
         unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
         ev = g_timer.begin(st);
@@ -392,6 +432,25 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
         CK(launch_ccf_peak(ws.sbj_sp.p, ws.ref_sp.p, ws.tw.p, g.NR, g.S, g.R, n, p0, g.P, ws.shifts_f.p, d_base, d_out,
                            d_peak, ws.err.p, st));
         g_timer.end(K_CCF, ev, st);
+        if (host)
+            CK(cudaEventRecord(ws.chunk_done[slot], st));
+        // the previous chunk's results leave while this one computes (a copy
+        // to pageable memory returns when it is done, so it is issued after
+        // this chunk's launches)
+        if (host && prev_n) {
+            int rc2 = copy_back(prev_p0, prev_n, slot ^ 1u);
+            if (rc2)
+                return rc2;
+        }
+        prev_p0 = p0;
+        prev_n = n;
+        slot ^= 1u;
+    }
+    if (host && prev_n) {
+        int rc2 = copy_back(prev_p0, prev_n, slot ^ 1u);
+        if (rc2)
+            return rc2;
+        CK(cudaStreamSynchronize(ws.copy_stream));
     }
     return 0;
 }
@@ -409,8 +468,6 @@ struct State {
     float* d_out = nullptr;
     float4* d_peak = nullptr;
     float2* d_base = nullptr;
-    float* h_stage = nullptr; // pinned staging for image uploads
-    size_t h_stage_n = 0;
 } g_state;
 
 std::mutex g_api_mu;
@@ -422,63 +479,25 @@ void free_call_buffers(State& s)
     if (s.d_out) cudaFree(s.d_out);
     if (s.d_peak) cudaFree(s.d_peak);
     if (s.d_base) cudaFree(s.d_base);
-    if (s.h_stage) cudaFreeHost(s.h_stage);
     s.d_sbj = s.d_ref = s.d_out = nullptr;
     s.d_peak = nullptr;
     s.d_base = nullptr;
-    s.h_stage = nullptr;
-    s.h_stage_n = 0;
 }
 
-// copy n host images (pointer list) into a device stack through pinned memory
+// copy n host images (pointer list) into a device stack
 int upload_images(State& s, const float** imgs, unsigned n, unsigned D, float* dst)
 {
-    const size_t img_elems = (size_t)D * D;
-    const size_t stage_imgs = 2048;
-    if (s.h_stage_n < 2 * stage_imgs * img_elems) {
-        if (s.h_stage)
-            cudaFreeHost(s.h_stage);
-        s.h_stage = nullptr;
-        s.h_stage_n = 0;
-        CK(cudaMallocHost(&s.h_stage, 2 * stage_imgs * img_elems * sizeof(float)));
-        s.h_stage_n = 2 * stage_imgs * img_elems;
+    unsigned bad = 0;
+    cudaError_t e = upload_host_images(imgs, n, (size_t)D * D, dst, s.stream, &bad);
+    if (e == cudaErrorInvalidValue) {
+        set_error(E_ARG, "image pointer %u is NULL", bad);
+        return E_ARG;
     }
-    cudaEvent_t done[2];
-    CK(cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming));
-    int rc = 0;
-    for (unsigned i0 = 0, b = 0; i0 < n && !rc; i0 += (unsigned)stage_imgs, b ^= 1) {
-        unsigned m = (unsigned)std::min<size_t>(stage_imgs, n - i0);
-        float* stage = s.h_stage + b * stage_imgs * img_elems;
-        cudaError_t e = cudaEventSynchronize(done[b]);
-        if (e != cudaSuccess) {
-            set_error(E_CUDA, "upload sync: %s", cudaGetErrorString(e));
-            rc = E_CUDA;
-            break;
-        }
-        for (unsigned i = 0; i < m; i++) {
-            if (!imgs[i0 + i]) {
-                set_error(E_ARG, "image pointer %u is NULL", i0 + i);
-                rc = E_ARG;
-                break;
-            }
-            std::memcpy(stage + i * img_elems, imgs[i0 + i], img_elems * sizeof(float));
-        }
-        if (rc)
-            break;
-        e = cudaMemcpyAsync(dst + (size_t)i0 * img_elems, stage, m * img_elems * sizeof(float), cudaMemcpyHostToDevice,
-                            s.stream);
-        if (e == cudaSuccess)
-            e = cudaEventRecord(done[b], s.stream);
-        if (e != cudaSuccess) {
-            set_error(E_CUDA, "image upload: %s", cudaGetErrorString(e));
-            rc = E_CUDA;
-        }
+    if (e != cudaSuccess) {
+        set_error(E_CUDA, "image upload: %s", cudaGetErrorString(e));
+        return E_CUDA;
     }
-    cudaStreamSynchronize(s.stream);
-    cudaEventDestroy(done[0]);
-    cudaEventDestroy(done[1]);
-    return rc;
+    return 0;
 }
 
 int do_multi_ref_align(State& s, const float** sbj_data, const float** ref_data, float* peak_list, float* d,
@@ -521,12 +540,10 @@ int do_multi_ref_align(State& s, const float** sbj_data, const float** ref_data,
         base[i] = make_float2(s.params[i].shift_x, s.params[i].shift_y);
     CK(cudaMemcpyAsync(s.d_base, base.data(), P * sizeof(float2), cudaMemcpyHostToDevice, s.stream));
 
-    rc = run_alignment(s.cfg, g, s.ws, s.d_sbj, s.d_ref, s.d_base, s.d_out, s.d_peak, mem_request, s.stream);
+    HostOut host{d, d_pitch, peak_list};
+    rc = run_alignment(s.cfg, g, s.ws, s.d_sbj, s.d_ref, s.d_base, s.d_out, s.d_peak, mem_request, s.stream, &host);
     if (rc)
         return rc;
-    CK(cudaMemcpy2DAsync(d, (size_t)d_pitch * sizeof(float), s.d_out, (size_t)P * sizeof(float), P * sizeof(float), R,
-                         cudaMemcpyDeviceToHost, s.stream));
-    CK(cudaMemcpyAsync(peak_list, s.d_peak, (size_t)R * P * sizeof(float4), cudaMemcpyDeviceToHost, s.stream));
     CK(cudaStreamSynchronize(s.stream));
     g_timer.collect();
     rc = check_device_flag(s.ws);
@@ -662,6 +679,7 @@ void gpu_clear(void)
     }
     gpuisac::prealign_clear();
     gpuisac::multigroup_clear();
+    gpuisac::release_upload_staging();
 }
 
 void reset_shifts(float shift_range, float shift_step)

@@ -40,6 +40,16 @@ std::vector<float2> shift_grid_of(float rx, float ry, float step);
 int prealign_reset_shifts(float shift_range, float shift_step);
 void prealign_clear();
 
+// Copies n host images of img_elems floats (one pointer per image) into the
+// device stack dst on `stream` and waits for the copies (host_upload.cu):
+// runs of images adjacent in host memory straight from the caller's memory,
+// scattered images through pinned staging.  A NULL image pointer returns
+// cudaErrorInvalidValue with its index in *bad.
+cudaError_t upload_host_images(const float* const* imgs, unsigned n, size_t img_elems, float* dst,
+                               cudaStream_t stream, unsigned* bad);
+// Frees the pinned staging area (gpu_clear).
+void release_upload_staging();
+
 // The multigroup session (multigroup.cu), likewise.
 int multigroup_reset_shifts(float shift_range, float shift_step);
 void multigroup_clear();

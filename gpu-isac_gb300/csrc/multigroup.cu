@@ -303,31 +303,15 @@ int upload_shift_tables(MgState& s)
     return 0;
 }
 
-// copy n host images (pointers) into the device stack dst through pinned memory
+// copy n host images (pointers) into the device stack dst
 int upload_images(const float** imgs, unsigned n, unsigned D, float* dst)
 {
-    const size_t img = (size_t)D * D;
-    const size_t stage = std::min<size_t>(n, 1024);
-    float* h = nullptr;
-    MG_CK(cudaMallocHost(&h, stage * img * sizeof(float)));
-    int rc = 0;
-    for (unsigned i0 = 0; i0 < n && rc == 0; i0 += (unsigned)stage) {
-        const unsigned m = (unsigned)std::min<size_t>(stage, n - i0);
-        for (unsigned i = 0; i < m; i++) {
-            if (!imgs[i0 + i]) {
-                rc = fail(E_ARG, "image pointer is NULL");
-                break;
-            }
-            std::memcpy(h + i * img, imgs[i0 + i], img * sizeof(float));
-        }
-        if (rc == 0) {
-            cudaError_t e = cudaMemcpy(dst + i0 * img, h, m * img * sizeof(float), cudaMemcpyHostToDevice);
-            if (e != cudaSuccess)
-                rc = fail(1, "image upload failed in the multigroup alignment");
-        }
-    }
-    cudaFreeHost(h);
-    return rc;
+    unsigned bad = 0;
+    cudaError_t e = upload_host_images(imgs, n, (size_t)D * D, dst, 0, &bad);
+    if (e == cudaErrorInvalidValue)
+        return fail(E_ARG, "image pointer is NULL");
+    MG_CK(e);
+    return 0;
 }
 
 // one iteration: alignment of every particle to its class average, the

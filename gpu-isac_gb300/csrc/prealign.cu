@@ -81,8 +81,6 @@ struct PreState {
     DBuf<float4> peak;
     DBuf<unsigned> err;
     TexStack sbj_tex;
-    float* h_stage = nullptr;
-    size_t h_stage_n = 0;
     std::vector<float4> h_peak;
     std::vector<float2> h_base;
 } g_pre;
@@ -103,10 +101,6 @@ void clear_pre(PreState& s)
     s.peak.release();
     s.err.release();
     s.sbj_tex.release();
-    if (s.h_stage)
-        cudaFreeHost(s.h_stage);
-    s.h_stage = nullptr;
-    s.h_stage_n = 0;
     std::free(s.params);
     s.params = nullptr;
     s.active = false;
@@ -134,28 +128,14 @@ int upload_shift_tables(PreState& s)
     return 0;
 }
 
-// copy n host images into the device stack dst through pinned memory
+// copy n host images into the device stack dst
 int upload(PreState& s, const float** imgs, unsigned n, float* dst)
 {
-    const size_t img_elems = (size_t)s.geo.D * s.geo.D;
-    const size_t stage_imgs = std::min<size_t>(n, 1024);
-    if (s.h_stage_n < stage_imgs * img_elems) {
-        if (s.h_stage)
-            cudaFreeHost(s.h_stage);
-        s.h_stage = nullptr;
-        s.h_stage_n = 0;
-        PRE_CK(cudaMallocHost(&s.h_stage, stage_imgs * img_elems * sizeof(float)));
-        s.h_stage_n = stage_imgs * img_elems;
-    }
-    for (unsigned i0 = 0; i0 < n; i0 += (unsigned)stage_imgs) {
-        const unsigned m = (unsigned)std::min<size_t>(stage_imgs, n - i0);
-        for (unsigned i = 0; i < m; i++) {
-            if (!imgs[i0 + i])
-                return fail(E_ARG, "image pointer is NULL");
-            std::memcpy(s.h_stage + i * img_elems, imgs[i0 + i], img_elems * sizeof(float));
-        }
-        PRE_CK(cudaMemcpy(dst + i0 * img_elems, s.h_stage, m * img_elems * sizeof(float), cudaMemcpyHostToDevice));
-    }
+    unsigned bad = 0;
+    cudaError_t e = upload_host_images(imgs, n, (size_t)s.geo.D * s.geo.D, dst, 0, &bad);
+    if (e == cudaErrorInvalidValue)
+        return fail(E_ARG, "image pointer is NULL");
+    PRE_CK(e);
     return 0;
 }
 

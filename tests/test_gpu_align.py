@@ -175,3 +175,34 @@ def test_texture_unit_matches_emulation(gpulib, cuda, monkeypatch, P, D, NR, bas
     assert (np.abs(d1 - d0) / np.maximum(np.abs(d0), 1e-30)).max() <= 1e-5
     same = (p1[..., 1:] == p0[..., 1:]).all(-1) & (circ_diff(p1[..., 0], p0[..., 0]) < ANGLE_TOL)
     assert same.mean() >= 0.995, same.mean()
+
+
+def test_host_abi_scattered_image_pointers(gpulib, cuda, small_case):
+    """multi_ref_align with image pointers that do not form runs in host
+    memory (the particles of a stack reached in a shuffled order, each copy
+    a separate array) goes through the pinned staging path; the result is
+    bit-identical to the contiguous call."""
+    import ctypes
+    from gpuisac import _lib, make_config, multi_ref_align
+    st = small_case
+    P, D, R = st.particles.shape[0], st.particles.shape[1], st.refs.shape[0]
+    pl0, d0 = multi_ref_align(st.particles, st.refs, 29, 2.0, 2.0)
+    # every particle its own allocation, allocated in a shuffled order
+    by_index = [None] * P
+    for i in np.random.default_rng(3).permutation(P):
+        by_index[i] = np.array(st.particles[i], copy=True)
+    fp = _lib.float_ptr
+    sp = (fp * P)(*[by_index[i].ctypes.data_as(fp) for i in range(P)])
+    keep = [np.array(st.refs[i], copy=True) for i in range(R)]
+    rp = (fp * R)(*[k.ctypes.data_as(fp) for k in keep])
+    L = _lib.load()
+    cfg = make_config(P, R, D, 29, 256, 1.0, 2.0, 2.0)
+    assert L.multi_ref_align_init(ctypes.byref(cfg), 0)
+    pl = np.zeros((R, 4 * P), np.float32)
+    d = np.zeros((R, P), np.float32)
+    try:
+        L.multi_ref_align(sp, rp, pl.ctypes.data_as(fp), d.ctypes.data_as(fp), P, ctypes.c_float(0.9))
+        _lib.check(L)
+    finally:
+        L.gpu_clear()
+    assert np.array_equal(d, d0) and np.array_equal(pl, pl0.reshape(R, 4 * P))
