@@ -577,7 +577,8 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
                 __syncthreads();
                 // ---- inverse FFT + peak search, one pair per 16-thread group ----
                 const unsigned s = s0 + g_shift;
-                if (s < n_shift)
+                // pairs of reference slots the group does not fill stay idle
+                if (s < n_shift && q0 + (unsigned)(g % QT) < grp.n_ref)
                     fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
             }
             if (failed)
@@ -622,7 +623,9 @@ constexpr int kWsBarF = 6;     // FFT side only (256 threads)
 // 16-thread FFT group per pair of the shift group (NSI shifts x 4 references).
 // NSI = 4 up to kTmaMaxRings rings; NSI = 2 halves the staging area for up
 // to kWsMaxRings rings (the references' tensor-memory columns bound both).
-template <int CW, int NSI>
+// QR: reference slots the contraction sums (4; 1 when every group of the
+// launch has one reference -- the other slots' pairs stay idle).
+template <int CW, int NSI, int QR>
 __global__ void __launch_bounds__(32 * CW + NSI * 64, 1)
 ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num, unsigned n_shift,
                    const float2* __restrict__ shifts_f, unsigned* __restrict__ err)
@@ -735,9 +738,9 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                         break;
                     }
                     phase ^= 1u;
-                    float acc[QT][SPT][4];
+                    float acc[QR][SPT][4];
 #pragma unroll
-                    for (int q = 0; q < QT; q++)
+                    for (int q = 0; q < QR; q++)
 #pragma unroll
                         for (int i = 0; i < SPT; i++)
 #pragma unroll
@@ -755,7 +758,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                         for (int jj = 0; jj < 2; jj++) {
                             if (j + jj < ring_num) {
 #pragma unroll
-                                for (int q = 0; q < QT; q++) {
+                                for (int q = 0; q < QR; q++) {
                                     const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
 #pragma unroll
                                     for (int i = 0; i < SPT; i++) {
@@ -817,7 +820,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
 #pragma unroll
                     for (int ii = 0; ii < SPT; ii++)
 #pragma unroll
-                        for (int q = 0; q < QT; q++)
+                        for (int q = 0; q < QR; q++)
                             write_z(zb + ((SPT * half + ii) * QT + q) * kPairStride, k, acc[q][ii][0], acc[q][ii][1],
                                     acc[q][ii][2], acc[q][ii][3]);
                     __threadfence_block();
@@ -868,7 +871,8 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     }
                     float2* gz = zbuf + (size_t)b * NP * kPairStride + g * kPairStride;
                     const unsigned s = s0 + g_shift;
-                    if (s < n_shift)
+                    // pairs of reference slots the group does not fill stay idle
+                    if (s < n_shift && q0 + (unsigned)(g % QT) < grp.n_ref)
                         fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
                     __threadfence_block();
                     nbar_arrive(kWsBarEmpty + b, NT);
@@ -1017,7 +1021,8 @@ ccf_peak_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_num
                 __syncthreads();
 
                 const unsigned s = s0 + g_shift;
-                if (s < n_shift)
+                // pairs of reference slots the group does not fill stay idle
+                if (s < n_shift && q0 + (unsigned)(g % QT) < grp.n_ref)
                     fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
             }
             merge_write(slots, st, tid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p, grp.p_total, shifts_f,
@@ -1049,18 +1054,18 @@ static size_t ws_smem_bytes(unsigned ring_num)
            kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16;
 }
 
-template <int CW, int NSI>
+template <int CW, int NSI, int QR>
 static cudaError_t launch_ws(const CcfWork& w, unsigned grid, const float2* twiddle, unsigned ring_num,
                              unsigned n_shift, const float2* shifts_f, unsigned* err, cudaStream_t stream)
 {
     static int configured = 0;
     if (!configured) {
-        cudaError_t e = set_max_smem(ccf_peak_ws_kernel<CW, NSI>);
+        cudaError_t e = set_max_smem(ccf_peak_ws_kernel<CW, NSI, QR>);
         if (e != cudaSuccess)
             return e;
         configured = 1;
     }
-    ccf_peak_ws_kernel<CW, NSI><<<grid, 32 * CW + NSI * 64, ws_smem_bytes(ring_num), stream>>>(
+    ccf_peak_ws_kernel<CW, NSI, QR><<<grid, 32 * CW + NSI * 64, ws_smem_bytes(ring_num), stream>>>(
         w, twiddle, ring_num, n_shift, shifts_f, err);
     return cudaSuccess;
 }
@@ -1170,13 +1175,21 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w, int variant, const float2* tw
     const unsigned grid = persistent_grid(w.n_items, 1);
     if (variant == kCcfWs) {
         const bool four = ccf_tile(ring_num, n_shift, true).ws_warps == 4;
+        const bool one_ref = w.max_ref == 1;
         cudaError_t e;
-        if (ring_num <= kTmaMaxRings)
-            e = four ? launch_ws<4, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream)
-                     : launch_ws<8, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
-        else
-            e = four ? launch_ws<4, 2>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream)
-                     : launch_ws<8, 2>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+        if (ring_num <= kTmaMaxRings) {
+            if (one_ref)
+                e = launch_ws<8, 4, 1>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+            else
+                e = four ? launch_ws<4, 4, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream)
+                         : launch_ws<8, 4, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+        } else {
+            if (one_ref)
+                e = launch_ws<8, 2, 1>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+            else
+                e = four ? launch_ws<4, 2, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream)
+                         : launch_ws<8, 2, 4>(w, grid, twiddle, ring_num, n_shift, shifts_f, err, stream);
+        }
         if (e != cudaSuccess)
             return e;
     } else if (variant == kCcfTmem) {
@@ -1244,6 +1257,7 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
     g.ref_tiles = (n_ref + qt - 1) / qt;
     g.rule = rule;
     w.n_items = g.ref_tiles * ((n_part + w.ppc - 1) / w.ppc);
+    w.max_ref = n_ref;
     return launch_ccf_peak_work(w, variant, twiddle, ring_num, n_shift, shifts_f, err, stream);
 }
 

@@ -106,7 +106,8 @@ struct CcfWork {
     CcfGroup one;
     unsigned n_groups;
     unsigned n_items;
-    unsigned ppc; // particles per work item
+    unsigned ppc;     // particles per work item
+    unsigned max_ref; // most references of any group (0: not known); 1 selects the one-reference contraction
 };
 
 enum { kCcfGeneral = 0, kCcfTmem = 1, kCcfWs = 2 };

@@ -405,6 +405,7 @@ int run_iteration(MgState& s)
         w.n_groups = cw.n_groups;
         w.n_items = cw.n_items;
         w.ppc = ppc;
+        w.max_ref = 1; // one reference (the class average) per group
         MG_CK(launch_ccf_peak_work(w, tile.variant, s.tw.p, NR, S, s.shifts_f.p, s.err.p, st));
     }
     s.h_peak.resize(P);
