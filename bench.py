@@ -140,10 +140,9 @@ class ClockSampler:
 
 
 def dist_setup(n_gpus):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    """(world, rank, local rank) of this process (gpuisac.replicas)."""
+    from gpuisac import replicas
+    return replicas.rank_env()
 
 
 def cpu_threads():
@@ -653,9 +652,8 @@ def bench_ours(args):
     spec_launches, spec_ms = n_l.value, t_l.value
     L.gpuisac_profile(0)
     if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+        from gpuisac import replicas
+        ms_total = replicas.max_over_ranks(ms_total, device=dev)
     ms_step = ms_total / args.steps
     alignments = P * R
     value = world * alignments / (ms_step / 1000.0)
@@ -714,9 +712,8 @@ def bench_ours(args):
                 times.append(dt)
         e2e_s = statistics.mean(times)
         if world > 1:
-            t = torch.tensor([e2e_s], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
+            from gpuisac import replicas
+            e2e_s = replicas.max_over_ranks(e2e_s, device=dev)
         h2d = (P + R) * w["img_dim"] ** 2 * 4 + P * 8
         d2h = R * P * 4 + R * P * 16
         e2e = {"value": world * alignments / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
