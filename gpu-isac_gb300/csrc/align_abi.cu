@@ -380,10 +380,8 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
     // both stacks as the reference's textures, sampled by the texture unit
     const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
     if (texture_unit_enabled()) {
-        CK(ws.ref_tex.build(refs, st));
-        CK(ws.sbj_tex.build(sbjs, st));
-        ref_tx = ws.ref_tex.objects();
-        sbj_tx = ws.sbj_tex.objects();
+        ref_tx = ws.ref_tex.try_build(refs, st);
+        sbj_tx = ws.sbj_tex.try_build(sbjs, st);
     }
     cudaEvent_t ev = g_timer.begin(st);
     CK(launch_polar_spectra(refs, ws.tmpl.p, ws.tw.p, g.NR, ws.zero_shift.p, 1, nullptr, 0,
@@ -796,10 +794,8 @@ int gpuisac_spectra_device_layout(const AlignConfig* cfg, const float* imgs, uns
         return rc;
     StackDesc sd{imgs, n_img, g.D, std::min(batch, std::max(n_img, 1u)), tex};
     const unsigned long long* tx = nullptr;
-    if (texture_unit_enabled() && n_img > 0) {
-        CK(ws.sbj_tex.build(sd, st));
-        tx = ws.sbj_tex.objects();
-    }
+    if (texture_unit_enabled() && n_img > 0)
+        tx = ws.sbj_tex.try_build(sd, st);
     CK(launch_polar_spectra(sd, ws.tmpl.p, ws.tw.p, g.NR, is_ref ? ws.zero_shift.p : ws.shifts_i.p, is_ref ? 1 : g.S,
                             reinterpret_cast<const float2*>(base_shift), 0, n_img, is_ref,
                             reinterpret_cast<float2*>(out), st, nullptr, tx));

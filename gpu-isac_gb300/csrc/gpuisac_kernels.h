@@ -50,6 +50,10 @@ struct TexStack {
     cudaError_t prepare(const StackDesc& st);
     cudaError_t fill(const StackDesc& st, cudaStream_t stream);
     cudaError_t build(const StackDesc& st, cudaStream_t stream);
+    // build(), or -- when it fails (no memory for the copy, say) -- nothing:
+    // returns the objects, or null after releasing any partial allocation;
+    // the caller then samples with the emulation, which computes the same taps
+    const unsigned long long* try_build(const StackDesc& st, cudaStream_t stream);
     const unsigned long long* objects() const { return d_objs; }
     void destroy_objects();
     void release();

@@ -151,7 +151,7 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     append(key, &st, sizeof(st));
     const CcfTile key_tile = ccf_tile(geo.NR, geo.S, true); // another tile shape records a new graph
     append(key, &key_tile, sizeof(key_tile));
-    const bool hw = texture_unit_enabled();
+    bool hw = texture_unit_enabled();
     append(key, &hw, sizeof(hw));
     if (S.plan.exec && S.plan.key == key) {
         G_CK(cudaMemsetAsync(S.err.p, 0, sizeof(unsigned), st));
@@ -190,14 +190,22 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     }
     S.ref_tex.resize(n_groups);
     S.sbj_tex.resize(n_groups);
-    if (hw)
-        for (unsigned gi = 0; gi < n_groups; gi++) {
-            const GpuisacGroup& g = groups[gi];
-            if (g.ref_num == 0 || g.sbj_num == 0)
-                continue;
-            G_CK(S.ref_tex[gi].prepare(ref_desc(g)));
-            G_CK(S.sbj_tex[gi].prepare(sbj_desc(g)));
+    // (a texture set that cannot be made -- no memory for the copies, say --
+    // leaves the whole plan on the emulation, which computes the same taps)
+    for (unsigned gi = 0; hw && gi < n_groups; gi++) {
+        const GpuisacGroup& g = groups[gi];
+        if (g.ref_num == 0 || g.sbj_num == 0)
+            continue;
+        if (S.ref_tex[gi].prepare(ref_desc(g)) != cudaSuccess ||
+            S.sbj_tex[gi].prepare(sbj_desc(g)) != cudaSuccess) {
+            (void)cudaGetLastError();
+            for (unsigned gj = 0; gj < n_groups; gj++) {
+                S.ref_tex[gj].release();
+                S.sbj_tex[gj].release();
+            }
+            hw = false;
         }
+    }
 
     size_t free_b = 0, total_b = 0;
     G_CK(cudaMemGetInfo(&free_b, &total_b));

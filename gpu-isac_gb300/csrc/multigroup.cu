@@ -330,13 +330,10 @@ int run_iteration(MgState& s)
     StackDesc refs{s.ref.p, R, D, R, s.tex};
     StackDesc sbjs{s.sbj.p, P, D, P, s.tex};
     const bool hw = texture_unit_enabled();
-    if (hw) {
-        MG_CK(s.ref_tex.build(refs, st));
-        if (!s.sbj_tex.objects())
-            MG_CK(s.sbj_tex.build(sbjs, st));
-    }
-    const unsigned long long* ref_tx = hw ? s.ref_tex.objects() : nullptr;
-    const unsigned long long* sbj_tx = hw ? s.sbj_tex.objects() : nullptr;
+    const unsigned long long* ref_tx = hw ? s.ref_tex.try_build(refs, st) : nullptr;
+    const unsigned long long* sbj_tx = nullptr;
+    if (hw)
+        sbj_tx = s.sbj_tex.objects() ? s.sbj_tex.objects() : s.sbj_tex.try_build(sbjs, st);
     MG_CK(launch_polar_spectra(refs, s.tmpl.p, s.tw.p, NR, s.zero.p, 1, nullptr, 0, R, 1, s.ref_sp.p, st, nullptr,
                                ref_tx));
 

@@ -330,10 +330,8 @@ void pre_align_run(int start_idx, int stop_idx)
         PRE_CK(s.sbj_sp.ensure(row * g.S * chunk));
         StackDesc sbjs{s.sbj.p, s.capacity, g.D, s.capacity, tex};
         const unsigned long long* sbj_tx = nullptr;
-        if (texture_unit_enabled()) {
-            PRE_CK(s.sbj_tex.build(sbjs, st));
-            sbj_tx = s.sbj_tex.objects();
-        }
+        if (texture_unit_enabled())
+            sbj_tx = s.sbj_tex.try_build(sbjs, st);
         for (unsigned c0 = 0; c0 < n; c0 += chunk) {
             const unsigned c = std::min(chunk, n - c0);
             PRE_CK(launch_polar_spectra(sbjs, s.tmpl.p, s.tw.p, g.NR, s.shifts_i.p, g.S, s.base.p, c0, c, 0,

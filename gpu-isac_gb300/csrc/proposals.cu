@@ -138,10 +138,8 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
     // reference spectra: every reference, stacked as the reference stacks them
     StackDesc refs{ref, geo.R, D, std::max(1u, std::min(geo.R, 100u)), tex};
     const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
-    if (texture_unit_enabled()) {
-        P_CK(S.ref_tex.build(refs, st));
-        ref_tx = S.ref_tex.objects();
-    }
+    if (texture_unit_enabled())
+        ref_tx = S.ref_tex.try_build(refs, st);
     P_CK(launch_polar_spectra(refs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, geo.R, 1, S.ref_sp.p, st, nullptr,
                               ref_tx));
 
@@ -156,10 +154,8 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
     P_CK(S.sbj_sp.ensure(row_elems * Sn * std::min(chunk, n_sel)));
     const float2* bs = reinterpret_cast<const float2*>(base_shift);
     StackDesc sbjs{sbj, geo.P, D, geo.sbj_batch, tex};
-    if (texture_unit_enabled()) {
-        P_CK(S.sbj_tex.build(sbjs, st));
-        sbj_tx = S.sbj_tex.objects();
-    }
+    if (texture_unit_enabled())
+        sbj_tx = S.sbj_tex.try_build(sbjs, st);
     const unsigned* sel_dev = part_idx;
     for (unsigned c0 = 0; c0 < n_sel; c0 += chunk) {
         const unsigned n = std::min(chunk, n_sel - c0);
@@ -328,10 +324,8 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
     // reference spectra for the search (reference basis, every reference)
     StackDesc refs{ref, R, D, std::max(1u, std::min(R, 100u)), tex};
     const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
-    if (texture_unit_enabled()) {
-        P_CK(S.ref_tex.build(refs, st));
-        ref_tx = S.ref_tex.objects();
-    }
+    if (texture_unit_enabled())
+        ref_tx = S.ref_tex.try_build(refs, st);
     P_CK(launch_polar_spectra(refs, S.tmpl.p, S.tw.p, NR, S.zero.p, 1, nullptr, 0, R, 1, S.ref_sp.p, st, nullptr,
                               ref_tx));
 
@@ -365,10 +359,8 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
 
     const float2* bs = reinterpret_cast<const float2*>(base_shift);
     StackDesc sbjs{sbj, P, D, geo.sbj_batch, tex};
-    if (texture_unit_enabled()) {
-        P_CK(S.sbj_tex.build(sbjs, st));
-        sbj_tx = S.sbj_tex.objects();
-    }
+    if (texture_unit_enabled())
+        sbj_tx = S.sbj_tex.try_build(sbjs, st);
     std::vector<CcfGroup> table(chunk);
     std::vector<unsigned> flags(chunk), fbl;
     unsigned long long n_pairs = 0;

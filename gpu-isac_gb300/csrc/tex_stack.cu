@@ -78,6 +78,15 @@ void TexStack::release()
     n = dim = batch = tex = 0;
 }
 
+const unsigned long long* TexStack::try_build(const StackDesc& st, cudaStream_t stream)
+{
+    if (build(st, stream) == cudaSuccess)
+        return d_objs;
+    (void)cudaGetLastError(); // allocation and launch-configuration errors are not sticky
+    release();
+    return nullptr;
+}
+
 cudaError_t TexStack::build(const StackDesc& st, cudaStream_t stream)
 {
     cudaError_t e = prepare(st);
