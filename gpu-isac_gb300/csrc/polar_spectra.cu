@@ -64,7 +64,7 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
     // sums, reduced in FP32 across each warp, feed the image mean / deviation
     // (the eight warp sums are added in FP64)
     float s1 = 0.f, s2 = 0.f;
-#pragma unroll 4
+#pragma unroll 8
     for (unsigned r = 0; r < ring_num; r++) {
         float2 o = __ldg(&tmpl[r * kRingLen + tid]);
         float x = cnt_x + o.x;
@@ -97,11 +97,14 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
         double nn = 0.5 * (double)ring_num * (double)(ring_num + 1) * (double)kRingLen;
         double avg = a / nn, msq = q / nn;
         double sd = sqrt(fabs(msq - avg * avg));
-        red[16] = avg;
-        red[17] = 1.0 / (sd + 0.0000001);
+        // stored as the floats every thread uses (one conversion, not 256)
+        float* redf = reinterpret_cast<float*>(red + 16);
+        redf[0] = (float)avg;
+        redf[1] = (float)(1.0 / (sd + 0.0000001));
     }
     __syncthreads();
-    const float avg_f = (float)red[16], inv_f = (float)red[17];
+    const float avg_f = reinterpret_cast<const float*>(red + 16)[0];
+    const float inv_f = reinterpret_cast<const float*>(red + 16)[1];
 
     // ---- per-ring FFT, two rings per complex 256-point FFT ----
     const int g = tid >> 4;          // FFT group 0..15
