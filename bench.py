@@ -562,6 +562,53 @@ def bench_multigroup(args, dev, L, st):
     return blk
 
 
+PREALIGN = {"workload": "pre-alignment: the 50,000 particles (76^2) against their mean, 35 rings, shift range 5 "
+                        "step 1 (121 shifts), one batch",
+            "rings": 35, "shift_range": 5.0, "shift_step": 1.0, "runs": 2}
+
+
+def bench_prealign(args, dev, L, st):
+    """pre_align_init, the particles fetched once, then per run the average
+    fetched and pre_align_run over all particles (ISAC's pre-alignment
+    iteration on one batch); value = particles aligned per second of run."""
+    import torch
+
+    from gpuisac import _lib
+    from gpuisac.align import make_config, ptr_array
+    m = PREALIGN
+    parts = np.ascontiguousarray(st.particles)
+    P, D = parts.shape[0], parts.shape[1]
+    avg = np.ascontiguousarray(parts.astype(np.float64).mean(0, keepdims=True).astype(np.float32))
+    cfg = make_config(P, 1, D, m["rings"], 256, m["shift_step"], m["shift_range"], m["shift_range"], b"pre_aln")
+    n_shift = L.gpuisac_shift_count(ctypes.byref(cfg))
+    t0 = time.perf_counter()
+    if not L.pre_align_init(P, ctypes.byref(cfg), torch.cuda.current_device()):
+        _lib_check(L)
+    L.pre_align_fetch(ptr_array(parts), P, b"sbj_batch")
+    _lib.check(L)
+    t_setup = time.perf_counter() - t0
+    runs = []
+    try:
+        for i in range(1 + m["runs"]):           # the first run is warm-up
+            t = time.perf_counter()
+            L.pre_align_fetch(ptr_array(avg), 1, b"ref_batch")
+            L.pre_align_run(0, P)
+            _lib.check(L)
+            if i:
+                runs.append(time.perf_counter() - t)
+    finally:
+        L.gpu_clear()
+    s_run = statistics.mean(runs)
+    blk = {"workload": m["workload"], "particles": P, "shifts": n_shift,
+           "value": P / s_run, "unit": "particles aligned/s (121 shifts x 256 angles x 2 mirrors, one reference)",
+           "ms_per_run": 1000.0 * s_run, "runs": len(runs), "init_and_particle_fetch_ms": 1000.0 * t_setup}
+    ref_t = os.path.join(ROOT, "tests", "golden", "ref_gpu_time_prealign.json")
+    if os.path.exists(ref_t):
+        r = json.load(open(ref_t))
+        blk["reference_library_ms_per_run"] = 1000.0 * min(r["seconds_per_run"])
+    return blk
+
+
 def _lib_check(L):
     from gpuisac import _lib
     _lib.check(L)
@@ -765,9 +812,11 @@ def bench_ours(args):
         big[cls, torch.arange(100000, device=dev)] += 0.3 * torch.rand(100000, generator=rng, device=dev)
         assign_blk["synthetic_100000x500"] = bench_assign(args, dev, L, big, cpu=False)
         del big
-    multigroup_blk = None
+    multigroup_blk = prealign_blk = None
     if rank == 0 and world == 1 and not args.no_multigroup and WORKLOAD["workload"].startswith("mref"):
         multigroup_blk = bench_multigroup(args, dev, L, st)
+    if rank == 0 and world == 1 and not args.no_prealign and WORKLOAD["workload"].startswith("mref"):
+        prealign_blk = bench_prealign(args, dev, L, st)
     if rank == 0 and world == 1 and not args.no_grouped:
         del d_out, peak_out
         torch.cuda.empty_cache()
@@ -787,7 +836,7 @@ def bench_ours(args):
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk,
-                "assign_groups": assign_blk, "multigroup": multigroup_blk}
+                "assign_groups": assign_blk, "multigroup": multigroup_blk, "prealign": prealign_blk}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -813,6 +862,7 @@ def main():
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped-launch comparison")
     ap.add_argument("--no-assign", action="store_true", help="skip the group-assignment block")
     ap.add_argument("--no-multigroup", action="store_true", help="skip the multigroup (stability test) block")
+    ap.add_argument("--no-prealign", action="store_true", help="skip the pre-alignment block")
     ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])
