@@ -225,13 +225,9 @@ __device__ __forceinline__ void phase_sync()
 // merge the nsi shift slots of each of the qt references and write the
 // outputs of particle p (the N threads of the FFT phase call, synchronised
 // by barrier BAR; threads < qt write)
-template <int BAR = 0, int N = 256>
-__device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st, int tid, int g, int l, int qt,
-                                            int nsi, unsigned q0, unsigned n_ref, unsigned n_shift, unsigned pg,
-                                            unsigned p_total, const float2* shifts_f, const float2* base,
-                                            float* d_out, float4* peak_out, unsigned rule = kPeakMref)
+// the running best of pair slot g into the shared slot array
+__device__ __forceinline__ void park_slot(PeakSlot* slots, const PeakState& st, int g, int l)
 {
-    phase_sync<BAR, N>();
     if (l == 0) {
         slots[g].v = st.bv;
         slots[g].h = st.bh;
@@ -239,6 +235,15 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
     }
     if (l < 7)
         slots[g].nb[l] = st.nb;
+}
+
+// the merge and the writes from slots every pair slot has parked
+template <int BAR = 0, int N = 256>
+__device__ __forceinline__ void merge_slots(PeakSlot* slots, int tid, int qt, int nsi, unsigned q0, unsigned n_ref,
+                                            unsigned n_shift, unsigned pg, unsigned p_total, const float2* shifts_f,
+                                            const float2* base, float* d_out, float4* peak_out,
+                                            unsigned rule = kPeakMref)
+{
     phase_sync<BAR, N>();
     if (tid < qt && q0 + tid < n_ref) {
         int best = tid;
@@ -260,6 +265,17 @@ __device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st
         peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
     }
     phase_sync<BAR, N>();
+}
+
+template <int BAR = 0, int N = 256>
+__device__ __forceinline__ void merge_write(PeakSlot* slots, const PeakState& st, int tid, int g, int l, int qt,
+                                            int nsi, unsigned q0, unsigned n_ref, unsigned n_shift, unsigned pg,
+                                            unsigned p_total, const float2* shifts_f, const float2* base,
+                                            float* d_out, float4* peak_out, unsigned rule = kPeakMref)
+{
+    phase_sync<BAR, N>();
+    park_slot(slots, st, g, l);
+    merge_slots<BAR, N>(slots, tid, qt, nsi, q0, n_ref, n_shift, pg, p_total, shifts_f, base, d_out, peak_out, rule);
 }
 
 // ---- mbarrier + bulk async copy (inline PTX) ----
@@ -650,6 +666,12 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
     const bool contraction_side = tid < NC;
+    // An item's (particle, shift) rows run through the shift groups as one
+    // stream, particle-major: with n_shift >= NSI a group may hold the end of
+    // one particle and the start of the next, so no group is left part empty
+    // at a particle's end.  Below NSI shifts every particle is padded to whole
+    // groups.  Row v of the item is particle v / vstride, shift v % vstride.
+    const unsigned vstride = n_shift >= (unsigned)NSI ? n_shift : (n_shift + NSI - 1) / NSI * NSI;
 
     unsigned item = blockIdx.x;
     CcfGroup grp;
@@ -681,17 +703,26 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
         // lane k of the tensor memory holds slot k; columns: [ring][ref][u, v]
         const uint32_t tmem = *tmem_slot + ((uint32_t)(32 * (warp & 3)) << 16);
         const uint32_t row_bytes = ring_num * kSlots * sizeof(float2);
-        auto issue = [&](const float2* sp, unsigned p, unsigned s0) {
-            unsigned nv = min((unsigned)NSI, n_shift - s0);
+        // the shift group of rows v0..v0+NSI-1 (item-local) of the item whose
+        // particles start at p0 and number np
+        auto issue = [&](const float2* sp, unsigned p0, unsigned np, unsigned v0) {
+            unsigned nv = 0;
+            for (unsigned i = 0; i < (unsigned)NSI; i++) {
+                const unsigned v = v0 + i, pl = v / vstride;
+                nv += (pl < np && v - pl * vstride < n_shift) ? 1u : 0u;
+            }
             fence_proxy_async();
             mbar_expect_tx(bar, nv * row_bytes);
-            for (unsigned i = 0; i < nv; i++)
-                bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sp + ((size_t)p * n_shift + s0 + i) * ring_num * kSlots,
-                         row_bytes, bar);
+            for (unsigned i = 0; i < (unsigned)NSI; i++) {
+                const unsigned v = v0 + i, pl = v / vstride, sv = v - pl * vstride;
+                if (pl < np && sv < n_shift)
+                    bulk_g2s(sbuf + (size_t)i * nrp * kSlots,
+                             sp + ((size_t)(p0 + pl) * n_shift + sv) * ring_num * kSlots, row_bytes, bar);
+            }
         };
         bool pending = false; // thread 0: copies in flight
         if (tid == 0) {
-            issue(grp.sbj_sp, pb, 0);
+            issue(grp.sbj_sp, pb, pe - pb, 0);
             pending = true;
         }
         unsigned it = 0;
@@ -720,8 +751,9 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             unsigned nq0 = 0, npb = 0, npe = 0;
             const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
 
-            for (unsigned p = pb; p < pe && !failed; p++) {
-                for (unsigned s0 = 0; s0 < n_shift; s0 += NSI, it++) {
+            const unsigned nrows = (pe - pb) * vstride;
+            for (unsigned v0 = 0; v0 < nrows && !failed; v0 += NSI, it++) {
+                {
                     const unsigned b = it & 1u;
                     // ---- wait for this group's spectra (bounded) ----
                     const bool ok = mbar_wait(bar, phase);
@@ -796,21 +828,11 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     nbar_sync(kWsBarC, NC); // the staging area is consumed
                     tmem_fence_after();
                     if (tid == 0) {
-                        const float2* n_sp = nullptr;
-                        unsigned n_p = 0, n_s0 = 0;
-                        if (s0 + NSI < n_shift) {
-                            n_sp = grp.sbj_sp;
-                            n_p = p;
-                            n_s0 = s0 + NSI;
-                        } else if (p + 1 < pe) {
-                            n_sp = grp.sbj_sp;
-                            n_p = p + 1;
+                        if (v0 + NSI < nrows) {
+                            issue(grp.sbj_sp, pb, pe - pb, v0 + NSI);
+                            pending = true;
                         } else if (has_next) {
-                            n_sp = ngrp.sbj_sp;
-                            n_p = npb;
-                        }
-                        if (n_sp) {
-                            issue(n_sp, n_p, n_s0);
+                            issue(ngrp.sbj_sp, npb, npe - npb, 0);
                             pending = true;
                         }
                     }
@@ -859,28 +881,44 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             CcfGroup ngrp;
             unsigned nq0 = 0, npb = 0, npe = 0;
             const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
-            for (unsigned p = pb; p < pe && !failed; p++) {
-                PeakState st;
-                st.reset(grp.rule);
-                for (unsigned s0 = 0; s0 < n_shift; s0 += NSI, it++) {
-                    const unsigned b = it & 1u;
-                    nbar_sync(kWsBarFull + b, NT);
-                    if (*abort_flag) {
-                        failed = true;
-                        break;
-                    }
-                    float2* gz = zbuf + (size_t)b * NP * kPairStride + g * kPairStride;
-                    const unsigned s = s0 + g_shift;
-                    // pairs of reference slots the group does not fill stay idle
-                    if (s < n_shift && q0 + (unsigned)(g % QT) < grp.n_ref)
-                        fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
-                    __threadfence_block();
-                    nbar_arrive(kWsBarEmpty + b, NT);
-                }
-                if (failed)
+            // st: the slot's running best of particle pb + pc, the particle of
+            // the shift group's first row.  In the group that holds pc's last
+            // row, a slot whose row already belongs to pc + 1 parks its best
+            // of pc before starting afresh, the others after their row; then
+            // the slots are merged for pc.
+            const unsigned nrows = (pe - pb) * vstride;
+            unsigned pc = 0;
+            PeakState st;
+            st.reset(grp.rule);
+            for (unsigned v0 = 0; v0 < nrows; v0 += NSI, it++) {
+                const unsigned b = it & 1u;
+                nbar_sync(kWsBarFull + b, NT);
+                if (*abort_flag) {
+                    failed = true;
                     break;
-                merge_write<kWsBarF, NF>(slots, st, ftid, g, l, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + p,
-                                     grp.p_total, shifts_f, grp.base, grp.d_out, grp.peak_out, grp.rule);
+                }
+                float2* gz = zbuf + (size_t)b * NP * kPairStride + g * kPairStride;
+                const unsigned v = v0 + g_shift, pl = v / vstride, s = v - pl * vstride;
+                const bool last = (pc + 1) * vstride <= v0 + NSI; // pc's last row is in this group
+                const bool next = pl != pc;                        // the same on both groups of a warp
+                if (last && next) {
+                    park_slot(slots, st, g, l);
+                    st.reset(grp.rule);
+                }
+                // pairs of reference slots the group does not fill stay idle
+                if (v < nrows && s < n_shift && q0 + (unsigned)(g % QT) < grp.n_ref)
+                    fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
+                __threadfence_block();
+                nbar_arrive(kWsBarEmpty + b, NT);
+                if (last) {
+                    if (!next) {
+                        park_slot(slots, st, g, l);
+                        st.reset(grp.rule);
+                    }
+                    merge_slots<kWsBarF, NF>(slots, ftid, QT, NSI, q0, grp.n_ref, n_shift, grp.p_first + pb + pc,
+                                             grp.p_total, shifts_f, grp.base, grp.d_out, grp.peak_out, grp.rule);
+                    pc++;
+                }
             }
             if (failed || !has_next)
                 break;
