@@ -42,8 +42,8 @@ void prealign_clear();
 
 // Copies n host images of img_elems floats (one pointer per image) into the
 // device stack dst on `stream` and waits for the copies (host_upload.cu):
-// runs of images adjacent in host memory straight from the caller's memory,
-// scattered images through pinned staging.  A NULL image pointer returns
+// pageable images through pinned staging filled by several host threads, a
+// contiguous pinned stack directly.  A NULL image pointer returns
 // cudaErrorInvalidValue with its index in *bad.
 cudaError_t upload_host_images(const float* const* imgs, unsigned n, size_t img_elems, float* dst,
                                cudaStream_t stream, unsigned* bad);
