@@ -23,7 +23,7 @@ std::atomic<unsigned long long> g_kernel_launches{0};
 // smem offset (floats) of ring r's samples
 __device__ __forceinline__ unsigned polar_index(unsigned r) { return (r >> 1) * 2 * kPairStride + (r & 1) * kRingLen; }
 
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 5)
 polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
                      unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
                      const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
