@@ -206,3 +206,45 @@ def test_host_abi_scattered_image_pointers(gpulib, cuda, small_case):
     finally:
         L.gpu_clear()
     assert np.array_equal(d, d0) and np.array_equal(pl, pl0.reshape(R, 4 * P))
+
+
+@pytest.mark.parametrize("rx,ry", [(1.0, 0.0), (0.0, 1.0), (2.0, 1.0)])
+def test_shift_grids_across_ccf_kernels(gpulib, cuda, oracle_mod, monkeypatch, rx, ry):
+    """Asymmetric shift grids (3 and 15 shifts): below 4 shifts every
+    particle is padded to whole shift groups of the warp-specialised kernel,
+    above it groups hold the end of one particle and the start of the next;
+    the single-phase kernel runs each particle's shifts on their own.  Same
+    arithmetic, so bit-identical; 45 rings (2 shifts per group) against the
+    oracle."""
+    from gpuisac import multi_ref_align
+    st = synth.make_stack(23, 76, 6, 2, 0.1, 30.0, 77)
+    runs = {}
+    for sel, warps in (("", "8"), ("ws", "4"), ("tmem", "8")):
+        monkeypatch.setenv("GPUISAC_CCF_KERNEL", sel)
+        monkeypatch.setenv("GPUISAC_CCF_WS_WARPS", warps)
+        runs[sel] = multi_ref_align(st.particles, st.refs, 35, rx, ry)
+    monkeypatch.delenv("GPUISAC_CCF_KERNEL")
+    monkeypatch.delenv("GPUISAC_CCF_WS_WARPS")
+    for sel in ("ws", "tmem"):
+        assert np.array_equal(runs[""][0], runs[sel][0]) and np.array_equal(runs[""][1], runs[sel][1]), sel
+    import oracle
+    big = synth.make_stack(23, 96, 6, 2, 0.1, 38.0, 78)
+    pl, d = multi_ref_align(big.particles, big.refs, 45, rx, ry)
+    cfg = oracle.make_cfg(23, 6, 96, 45, 256, 1.0, rx, ry)
+    lay = oracle.reference_layout(cfg)
+    lay = oracle.OrcLayout(lay.sbj_batch, gpulib.get_texture_limit(96), lay.ref_batch)
+    peak_o, d_o = oracle_mod.multi_ref_align(cfg, lay, big.particles, big.refs)
+    compare(pl.reshape(6, 23, 4), d, peak_o, d_o)
+
+
+def test_pinned_host_stack_matches_pageable(gpulib, cuda, small_case):
+    """A contiguous stack in pinned host memory is copied straight to the
+    device; pageable stacks go through the pinned staging: same results."""
+    import torch
+    from gpuisac import multi_ref_align
+    st = small_case
+    pin = torch.empty(st.particles[:48].shape, dtype=torch.float32, pin_memory=True).numpy()
+    pin[...] = st.particles[:48]
+    a = multi_ref_align(st.particles[:48].copy(), st.refs, 29, 2.0, 2.0)
+    b = multi_ref_align(pin, st.refs, 29, 2.0, 2.0)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
