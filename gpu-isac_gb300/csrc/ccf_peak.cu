@@ -779,6 +779,12 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                             for (int c = 0; c < 4; c++)
                                 acc[q][i][c] = 0.f;
                     const float2* sb = sbuf + (size_t)(SPT * half) * nrp * kSlots + k;
+                    // The zero ring that pads an odd ring count is summed like
+                    // the others: it is zero in both the staging area and the
+                    // tensor memory, and an accumulator that starts at +0 is
+                    // never -0 under round-to-nearest, so adding 0 * 0 leaves
+                    // every sum bit for bit as it was (and the loop has no
+                    // per-ring branch).
                     auto ring_pair = [&](const float (&rv)[16], unsigned j) {
                         float2 pa[2][SPT];
 #pragma unroll
@@ -788,18 +794,16 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                                 pa[jj][i] = sb[(size_t)(i * nrp + j + jj) * kSlots];
 #pragma unroll
                         for (int jj = 0; jj < 2; jj++) {
-                            if (j + jj < ring_num) {
 #pragma unroll
-                                for (int q = 0; q < QR; q++) {
-                                    const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
+                            for (int q = 0; q < QR; q++) {
+                                const float u = rv[jj * 8 + 2 * q], vv = rv[jj * 8 + 2 * q + 1];
 #pragma unroll
-                                    for (int i = 0; i < SPT; i++) {
-                                        const float2 a = pa[jj][i];
-                                        acc[q][i][0] = fmaf(u, a.x, acc[q][i][0]);
-                                        acc[q][i][1] = fmaf(u, a.y, acc[q][i][1]);
-                                        acc[q][i][2] = fmaf(vv, a.y, acc[q][i][2]);
-                                        acc[q][i][3] = fmaf(vv, a.x, acc[q][i][3]);
-                                    }
+                                for (int i = 0; i < SPT; i++) {
+                                    const float2 a = pa[jj][i];
+                                    acc[q][i][0] = fmaf(u, a.x, acc[q][i][0]);
+                                    acc[q][i][1] = fmaf(u, a.y, acc[q][i][1]);
+                                    acc[q][i][2] = fmaf(vv, a.y, acc[q][i][2]);
+                                    acc[q][i][3] = fmaf(vv, a.x, acc[q][i][3]);
                                 }
                             }
                         }
