@@ -809,24 +809,26 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                         }
                     };
                     {
+                        // four rings per iteration, the next ring pair's
+                        // columns in flight; the load after the last pair
+                        // re-reads that pair (address clamped inside the
+                        // allocation) instead of a branch; an odd last pair
+                        // of rings follows the loop
                         float ra[16], rb[16];
                         tmem_ld16_async(tmem, ra);
                         tmem_wait_ld16(ra);
-                        for (unsigned j = 0; j < nrp; j += 4) {
-                            const bool more_b = j + 2 < nrp;
-                            if (more_b)
-                                tmem_ld16_async(tmem + (j + 2) * 8, rb);
+                        const unsigned n4 = nrp >> 2;
+                        for (unsigned t = 0; t < n4; t++) {
+                            const unsigned j = 4 * t;
+                            tmem_ld16_async(tmem + (j + 2) * 8, rb);
                             ring_pair(ra, j);
-                            if (!more_b)
-                                break;
                             tmem_wait_ld16(rb);
-                            const bool more_a = j + 4 < nrp;
-                            if (more_a)
-                                tmem_ld16_async(tmem + (j + 4) * 8, ra);
+                            tmem_ld16_async(tmem + min(j + 4, nrp - 2) * 8, ra);
                             ring_pair(rb, j + 2);
-                            if (more_a)
-                                tmem_wait_ld16(ra);
+                            tmem_wait_ld16(ra);
                         }
+                        if (nrp & 2u)
+                            ring_pair(ra, nrp - 2);
                     }
                     tmem_fence_before();
                     nbar_sync(kWsBarC, NC); // the staging area is consumed
