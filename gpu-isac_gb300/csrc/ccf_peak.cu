@@ -294,26 +294,25 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
+// try_wait suspends the thread until the phase completes or the hinted time
+// (ns) has passed, leaving the issue slots to the other warps meanwhile
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity, uint32_t hint_ns)
 {
     uint32_t ok;
     asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(ok)
-                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
                  : "memory");
     return ok != 0;
 }
-
-// bounded wait: gives up after ~2^22 polls (about a second with the back-off)
+// bounded wait: gives up after 2^16 tries of at most 20 us (about a second)
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
 {
-    for (uint32_t it = 0; it < (1u << 22); it++) {
-        if (mbar_test(bar, parity))
+    for (uint32_t it = 0; it < (1u << 16); it++)
+        if (mbar_try(bar, parity, 20000u))
             return true;
-        __nanosleep(it < 64 ? 0 : 256);
-    }
     return false;
 }
 
