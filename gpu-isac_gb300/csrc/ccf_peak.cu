@@ -130,6 +130,8 @@ __device__ __forceinline__ void write_z(float2* zp, int k, float a1, float a2, f
 }
 
 // inverse FFT of the pair in gz and the peak search of both mirrors
+// (kTwl: tw is this thread's row of precomputed twiddles, fft256_group_twl)
+template <bool kTwl = false>
 __device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, unsigned gmask, unsigned s,
                                          unsigned n_shift, PeakState& st, unsigned rule = kPeakMref)
 {
@@ -137,7 +139,10 @@ __device__ __forceinline__ void fft_peak(float2* gz, const float2* tw, int l, un
 #pragma unroll
     for (int m = 0; m < 16; m++)
         x[m] = gz[l + 16 * m];
-    fft256_group<+1>(x, gz, tw, l, gmask);
+    if (kTwl)
+        fft256_group_twl<+1>(x, gz, tw, gmask);
+    else
+        fft256_group<+1>(x, gz, tw, l, gmask);
     float* wf = reinterpret_cast<float*>(gz);
     if (rule == kPeakPreAlign && s == 0 && st.bv == 0.f && st.bh == 0 && st.bt == 0) {
         // the starting index (normal, shift 0, angle 0) stays the answer when
@@ -656,8 +661,8 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
     const unsigned nrp = 2 * ((ring_num + 1) / 2); // rings per staged shift (one zero ring if odd)
     float2* sbuf = reinterpret_cast<float2*>(smem_raw);                // [NSI][nrp][kSlots]
     float2* zbuf = sbuf + (size_t)NSI * nrp * kSlots;                  // [2][NP][kPairStride]
-    float2* tw = zbuf + 2 * NP * kPairStride;                          // [256]
-    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + kRingLen);      // [16]
+    float2* tw = zbuf + 2 * NP * kPairStride;                          // [16][kTwRow] per FFT lane
+    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);   // [16]
     uint64_t* bar = reinterpret_cast<uint64_t*>(slots + 16);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -678,8 +683,11 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
     if (!decode_item(w, item, QT, grp, q0, pb, pe))
         return;
 
-    if (tid < kRingLen)
-        tw[tid] = twiddle[tid];
+    if (tid < kRingLen) { // lane l's inverse-FFT twiddles, row l
+        const int tl = tid >> 4, tj = tid & 15;
+        const float2 t = twiddle[(tl * tj) & (kRingLen - 1)];
+        tw[tl * kTwRow + tj] = make_float2(t.x, t.y * -1.f);
+    }
     for (unsigned i = tid; i < (unsigned)NSI * nrp * kSlots; i += NT)
         sbuf[i] = make_float2(0.f, 0.f); // the padding ring stays zero
     if (warp == 0)
@@ -912,7 +920,7 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                 }
                 // pairs of reference slots the group does not fill stay idle
                 if (v < nrows && s < n_shift && q0 + (unsigned)(g % QT) < grp.n_ref)
-                    fft_peak(gz, tw, l, gmask, s, n_shift, st, grp.rule);
+                    fft_peak<true>(gz, tw + l * kTwRow, l, gmask, s, n_shift, st, grp.rule);
                 __threadfence_block();
                 nbar_arrive(kWsBarEmpty + b, NT);
                 if (last) {
@@ -1094,7 +1102,7 @@ static size_t ws_smem_bytes(unsigned ring_num)
 {
     const unsigned nrp = 2 * ((ring_num + 1) / 2), nsi = ws_shifts_per_group(ring_num);
     return (size_t)nsi * nrp * kSlots * sizeof(float2) + 2 * nsi * 4 * kPairStride * sizeof(float2) +
-           kRingLen * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16;
+           16 * kTwRow * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16;
 }
 
 template <int CW, int NSI, int QR>

@@ -114,6 +114,31 @@ __device__ __forceinline__ void fft256_group(float2 (&x)[16], float2* ws, const 
     dft16<SIGN>(x);
 }
 
+// The same FFT with this thread's twiddles precomputed: twl[j] = the factor
+// fft256_group applies to output j of thread l (the table's e^(-2 pi i l j / 256)
+// with the sign of SIGN), read at fixed offsets instead of through (l j) & 255.
+// Rows of 17 float2 keep the 16 threads of a group on distinct banks.
+constexpr int kTwRow = 17;
+template <int SIGN>
+__device__ __forceinline__ void fft256_group_twl(float2 (&x)[16], float2* ws, const float2* twl, unsigned mask)
+{
+    const int l = threadIdx.x & 15;
+    dft16<SIGN>(x);
+#pragma unroll
+    for (int j = 1; j < 16; j++)
+        x[perm16(j)] = cmul(x[perm16(j)], twl[j]);
+    __syncwarp(mask);
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+        ws[l * 17 + j] = x[perm16(j)];
+    __syncwarp(mask);
+#pragma unroll
+    for (int n = 0; n < 16; n++)
+        x[n] = ws[n * 17 + l];
+    __syncwarp(mask);
+    dft16<SIGN>(x);
+}
+
 // ---------------------------------------------------------------------------
 // Stacked image arrays read the way the reference's 2D textures are read
 // (bilinear, clamp, unnormalised coordinates; cuda/gpu_aln_noref.cu:1258-1286,
