@@ -7,7 +7,8 @@
 // C2R of every ccf-table entry (:2453-2461), cu_aln_param_wizard (:1667-1794)
 // and the host scatter of multi_ref_align (:516-541).
 //
-// Both kernels run 256 threads and 16 (shift, reference) pairs per iteration:
+// Every kernel runs 16 (shift, reference) pairs per shift group (8 with 2
+// shifts per group) through three stages:
 //   contraction  the four sums that form Z[k] and Z[256-k] (Z = O + iM, see
 //                polar_spectra.cu) for every slot k;
 //   inverse FFT  16 groups of 16 threads, one 256-point FFT per pair; real part
@@ -17,6 +18,11 @@
 //                with the 7 samples around it; merged per reference at the
 //                end of the particle, then the 7-point parabola.
 //
+// ccf_peak_ws_kernel<CW, NSI, QR> (up to 64 rings; the default): warp-
+//   specialised, CW contraction warps with the 4 references in tensor memory
+//   and the subject spectra staged by bulk async copies, and one 16-thread
+//   FFT / peak group per pair running the previous shift group at the same
+//   time; an item's (particle, shift) rows stream through the shift groups.
 // ccf_peak_tmem_kernel (up to 36 rings): 4 references per CTA held in tensor
 //   memory (lane = spectrum slot k, which is exactly the lane the thread
 //   owning slot k may read), split by ring halves across the two 128-thread
