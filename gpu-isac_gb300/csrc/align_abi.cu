@@ -114,7 +114,7 @@ int validate(const AlignConfig* cfg, Geometry& g, bool need_type)
         return E_UNSUPPORTED;
     }
     if (cfg->ring_len != (unsigned)kRingLen) {
-        set_error(E_UNSUPPORTED, "ring_len %u unsupported (this build computes 256-sample rings)", cfg->ring_len);
+        set_error(E_UNSUPPORTED, "ring_len %u unsupported (this library computes 256-sample rings)", cfg->ring_len);
         return E_UNSUPPORTED;
     }
     if (cfg->ring_num == 0 || cfg->ring_num > kMaxRingNum) {
