@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -20,6 +21,7 @@
 
 #include "../../include/gpu_aln_pack.h"
 #include "gpuisac_kernels.h"
+#include "gpuisac_split.h"
 #include "host_geometry.h"
 
 using namespace gpuisac;
@@ -216,6 +218,8 @@ struct Workspace {
     DevBuf<float2> tmpl, tw, shifts_f, ref_sp, sbj_sp, base;
     DevBuf<int2> shifts_i, zero_shift;
     DevBuf<unsigned> err; // device-side timeout flag of the kernels' bounded waits
+    DevBuf<unsigned char> sop, rop; // BF16 hi/lo operands of the tensor-core contraction
+    DevBuf<float2> zsp;             // its pair spectra
     TexStack ref_tex, sbj_tex; // the stacks as textures for the texture unit
     cudaStream_t copy_stream = nullptr; // results to the host, overlapping the next chunk
     cudaEvent_t chunk_done[2] = {nullptr, nullptr};
@@ -230,6 +234,9 @@ struct Workspace {
             cudaStreamDestroy(copy_stream);
         copy_stream = nullptr;
         err.release();
+        sop.release();
+        rop.release();
+        zsp.release();
         ref_tex.release();
         sbj_tex.release();
         geo_D = geo_NR = 0;
@@ -303,8 +310,8 @@ struct KernelTimer {
         cudaEvent_t a, b;
     };
     std::vector<Pending> pending;
-    unsigned long long launches[2] = {0, 0};
-    double ms[2] = {0.0, 0.0};
+    unsigned long long launches[4] = {0, 0, 0, 0};
+    double ms[4] = {0.0, 0.0, 0.0, 0.0};
     cudaEvent_t begin(cudaStream_t st)
     {
         if (!on)
@@ -342,7 +349,27 @@ struct KernelTimer {
         pending.clear();
     }
 } g_timer;
-enum { K_SPECTRA = 0, K_CCF = 1 };
+enum { K_SPECTRA = 0, K_CCF = 1, K_MMA = 2, K_ZFFT = 3 };
+
+// ---------------------------------------------------------------- contraction
+// Arithmetic of the ring-summed contraction: FP32 on the CUDA cores (the
+// drop-in default) or BF16 hi/lo split on the tensor cores.  The environment
+// variable GPUISAC_CONTRACTION=bf16x3 selects the latter at load time, so an
+// unchanged caller of the reference's entry points can opt in.
+std::atomic<int> g_contraction{-1};
+
+int contraction_mode()
+{
+    int m = g_contraction.load();
+    if (m < 0) {
+        const char* e = getenv("GPUISAC_CONTRACTION");
+        m = (e && std::strcmp(e, "bf16x3") == 0) ? GPUISAC_CONTRACTION_BF16X3 : GPUISAC_CONTRACTION_FP32;
+        int expected = -1;
+        g_contraction.compare_exchange_strong(expected, m);
+        m = g_contraction.load();
+    }
+    return m;
+}
 
 // ---------------------------------------------------------------- the pipeline
 // Host destinations of the results (the reference-facing call): d [R][pitch]
@@ -352,6 +379,104 @@ struct HostOut {
     unsigned d_pitch = 0;
     float* peak = nullptr;
 };
+
+// results of particles c0 .. c0 + cn - 1 to the host (copy stream, after the
+// chunk's kernels: event ev)
+int copy_chunk_back(const Geometry& g, Workspace& ws, const HostOut* host, const float* d_out, const float4* d_peak,
+                    unsigned c0, unsigned cn, cudaEvent_t ev)
+{
+    CK(cudaStreamWaitEvent(ws.copy_stream, ev, 0));
+    CK(cudaMemcpy2DAsync(host->d + c0, (size_t)host->d_pitch * sizeof(float), d_out + c0, (size_t)g.P * sizeof(float),
+                         (size_t)cn * sizeof(float), g.R, cudaMemcpyDeviceToHost, ws.copy_stream));
+    CK(cudaMemcpy2DAsync(host->peak + 4 * (size_t)c0, (size_t)g.P * sizeof(float4), d_peak + c0,
+                         (size_t)g.P * sizeof(float4), (size_t)cn * sizeof(float4), g.R, cudaMemcpyDeviceToHost,
+                         ws.copy_stream));
+    return 0;
+}
+
+int prepare_copy_back(Workspace& ws)
+{
+    if (!ws.copy_stream)
+        CK(cudaStreamCreateWithFlags(&ws.copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++)
+        if (!ws.chunk_done[i])
+            CK(cudaEventCreateWithFlags(&ws.chunk_done[i], cudaEventDisableTiming));
+    return 0;
+}
+
+// The same alignment with the contraction on the tensor cores: reference
+// operands once, then per particle chunk the subject operands, the MMA kernel
+// (pair spectra to HBM) and the inverse-FFT / peak kernel.
+int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs, const StackDesc& sbjs,
+                        const unsigned long long* ref_tx, const unsigned long long* sbj_tx, const float2* d_base,
+                        float* d_out, float4* d_peak, float mem_request, cudaStream_t st, const HostOut* host)
+{
+    SplitPlan pl;
+    if (!split_plan(g.NR, g.S, g.R, pl)) {
+        set_error(E_UNSUPPORTED, "the tensor-core contraction has no tile plan for %u rings, %u shifts, %u references",
+                  g.NR, g.S, g.R);
+        return E_UNSUPPORTED;
+    }
+    if (ws.rop.ensure(split_rop_bytes(pl)))
+        return E_NOMEM;
+    cudaEvent_t ev = g_timer.begin(st);
+    CK(launch_polar_operands(refs, ws.tmpl.p, ws.tw.p, g.NR, ws.zero_shift.p, 1, nullptr, 0, g.R, 1,
+                             split_ref_layout(pl, ws.rop.p), st, ref_tx));
+    g_timer.end(K_SPECTRA, ev, st);
+    // particle chunk: operands and pair spectra of a particle (21 MB at 76²,
+    // 35 rings, 49 shifts, 200 references) within the requested share of
+    // free memory, at most 2,048 particles
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const double frac = (mem_request > 0.f && mem_request <= 1.f) ? mem_request : 0.9;
+    const size_t budget = (size_t)((double)free_b * frac) / 2;
+    const size_t per_part = split_sop_bytes(pl, 1) + split_z_bytes(pl, 1, g.R);
+    size_t chunk = std::max<size_t>(1, std::min<size_t>(budget / per_part, 2048));
+    chunk = std::min<size_t>(chunk, g.P);
+    if (ws.sop.ensure(split_sop_bytes(pl, (unsigned)chunk)) ||
+        ws.zsp.ensure(split_z_bytes(pl, (unsigned)chunk, g.R) / sizeof(float2)) || ws.err.ensure(1))
+        return E_NOMEM;
+    CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), st));
+    if (host) {
+        int rc = prepare_copy_back(ws);
+        if (rc)
+            return rc;
+    }
+    const OperandLayout sl = split_sbj_layout(pl, ws.sop.p);
+    unsigned prev_p0 = 0, prev_n = 0, slot = 0;
+    for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk) {
+        const unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
+        ev = g_timer.begin(st);
+        CK(launch_polar_operands(sbjs, ws.tmpl.p, ws.tw.p, g.NR, ws.shifts_i.p, g.S, d_base, p0, n, 0, sl, st,
+                                 sbj_tx));
+        g_timer.end(K_SPECTRA, ev, st);
+        ev = g_timer.begin(st);
+        CK(launch_ccf_mma(pl, ws.sop.p, ws.rop.p, ws.zsp.p, n, g.R, g.S, ws.err.p, st));
+        g_timer.end(K_MMA, ev, st);
+        ev = g_timer.begin(st);
+        CK(launch_zfft_peak(pl, ws.zsp.p, n, p0, g.P, g.R, g.S, ws.tw.p, ws.shifts_f.p, d_base, d_out, d_peak,
+                            ws.err.p, st));
+        g_timer.end(K_ZFFT, ev, st);
+        if (host) {
+            CK(cudaEventRecord(ws.chunk_done[slot], st));
+            if (prev_n) {
+                int rc = copy_chunk_back(g, ws, host, d_out, d_peak, prev_p0, prev_n, ws.chunk_done[slot ^ 1u]);
+                if (rc)
+                    return rc;
+            }
+        }
+        prev_p0 = p0;
+        prev_n = n;
+        slot ^= 1u;
+    }
+    if (host && prev_n) {
+        int rc = copy_chunk_back(g, ws, host, d_out, d_peak, prev_p0, prev_n, ws.chunk_done[slot ^ 1u]);
+        if (rc)
+            return rc;
+        CK(cudaStreamSynchronize(ws.copy_stream));
+    }
+    return 0;
+}
 
 // Device-resident multi-reference alignment of P particles against R refs.
 // With host destinations, each chunk's columns are copied back on a second
@@ -374,15 +499,17 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
     StackDesc refs{d_ref, g.R, g.D, ref_batch, tex};
     StackDesc sbjs{d_sbj, g.P, g.D, std::max(1u, reference_sbj_batch(cfg)), tex};
 
-    const size_t row_elems = (size_t)g.NR * kSlots; // float2 per (image, shift) row
-    if (ws.ref_sp.ensure(row_elems * std::max(g.R, 1u)))
-        return E_NOMEM;
     // both stacks as the reference's textures, sampled by the texture unit
     const unsigned long long *ref_tx = nullptr, *sbj_tx = nullptr;
     if (texture_unit_enabled()) {
         ref_tx = ws.ref_tex.try_build(refs, st);
         sbj_tx = ws.sbj_tex.try_build(sbjs, st);
     }
+    if (contraction_mode() == GPUISAC_CONTRACTION_BF16X3)
+        return run_alignment_split(g, ws, refs, sbjs, ref_tx, sbj_tx, d_base, d_out, d_peak, mem_request, st, host);
+    const size_t row_elems = (size_t)g.NR * kSlots; // float2 per (image, shift) row
+    if (ws.ref_sp.ensure(row_elems * std::max(g.R, 1u)))
+        return E_NOMEM;
     cudaEvent_t ev = g_timer.begin(st);
     CK(launch_polar_spectra(refs, ws.tmpl.p, ws.tw.p, g.NR, ws.zero_shift.p, 1, nullptr, 0,
                             g.R, 1, ws.ref_sp.p, st, nullptr, ref_tx));
@@ -857,12 +984,28 @@ int gpuisac_ccf_peak_device(const AlignConfig* cfg, const float* sbj_spectra, co
 
 unsigned long long gpuisac_launch_count(void) { return g_kernel_launches.load(); }
 
+int gpuisac_set_contraction(int mode)
+{
+    if (mode != GPUISAC_CONTRACTION_FP32 && mode != GPUISAC_CONTRACTION_BF16X3) {
+        set_error(E_ARG, "unknown contraction mode %d", mode);
+        return -1;
+    }
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    const int prev = contraction_mode();
+    g_contraction.store(mode);
+    return prev;
+}
+
+int gpuisac_get_contraction(void) { return contraction_mode(); }
+
 void gpuisac_profile(int on)
 {
     std::lock_guard<std::mutex> lk(g_api_mu);
     g_timer.on = on != 0;
-    g_timer.launches[0] = g_timer.launches[1] = 0;
-    g_timer.ms[0] = g_timer.ms[1] = 0.0;
+    for (int i = 0; i < 4; i++) {
+        g_timer.launches[i] = 0;
+        g_timer.ms[i] = 0.0;
+    }
 }
 
 int gpuisac_kernel_time(const char* kernel, unsigned long long* launches, double* total_ms)
@@ -873,6 +1016,10 @@ int gpuisac_kernel_time(const char* kernel, unsigned long long* launches, double
         k = K_SPECTRA;
     else if (kernel && std::strcmp(kernel, "ccf_peak") == 0)
         k = K_CCF;
+    else if (kernel && std::strcmp(kernel, "ccf_mma") == 0)
+        k = K_MMA;
+    else if (kernel && std::strcmp(kernel, "zfft_peak") == 0)
+        k = K_ZFFT;
     if (k < 0) {
         set_error(E_ARG, "unknown kernel name '%s'", kernel ? kernel : "(null)");
         return E_ARG;

@@ -1,0 +1,603 @@
+// ccf_split.cu -- the ring-summed cross-correlation on the tensor cores:
+// BF16 hi/lo split operands (hi*hi + hi*lo + lo*hi, FP32 accumulation in
+// tensor memory), then the inverse angular FFT and the peak search.
+//
+// Reference semantics: cu_ccf_mult_mref (cuda/gpu_aln_noref.cu:1483-1537),
+// the C2R of every ccf-table entry (:2453-2461) and cu_aln_param_wizard
+// (:1667-1794) -- the same as ccf_peak.cu, whose peak search and FFT this
+// file shares (ccf_device.cuh); only the contraction's arithmetic differs.
+//
+// For every spectrum slot k the contraction is a GEMM over the rings:
+//   D[(shift s, a|b)][(reference q, u|v)] = sum_r S[s][r][a|b] * R[q][r][u|v]
+// whose four products per (shift, reference) pair are Re/Im of Z[k] and of
+// Z[256-k] (polar_spectra.cu).  Every pair needs all 128 slots before its
+// inverse FFT, 2 KB of accumulators, so MMA-sized tiles (thousands of pairs)
+// cannot keep them on the SM: the pair spectra Z pass through HBM between two
+// kernels, each launched once per particle chunk:
+//
+// ccf_mma_kernel    persistent; work item = (particle, shift block, reference
+//                   tile); 192 threads: warp 0 issues the bulk copies of each
+//                   slot's operands into a ring of shared-memory stages, one
+//                   thread of warp 1 issues the 3 x K/16 tcgen05.mma of a slot
+//                   (M = 128 lanes = 64 shifts x {a, b}, N = 2 x references)
+//                   into one of two accumulators in tensor memory, and warps
+//                   2-5 drain the other accumulator with tcgen05.ld, pair the
+//                   a/b lanes by shuffle and write Z[k], Z[256-k] of every
+//                   (shift, reference) pair.
+// zfft_peak_kernel  persistent; work item = (particle, reference); the Z block
+//                   of each shift block is bulk-copied into one of two shared
+//                   buffers while the previous one is transformed; 16 threads
+//                   per shift run the inverse FFT and the peak search, the
+//                   shift slots are merged at the particle's end.
+//
+// Every wait is bounded (about a second); a kernel that gives up sets *err,
+// lets its own copies and MMAs land, frees its tensor memory and returns.
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "ccf_device.cuh"
+#include "gpuisac_device.cuh"
+#include "gpuisac_kernels.h"
+#include "gpuisac_split.h"
+
+namespace gpuisac {
+
+namespace {
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// bounded wait that also gives up once another role has aborted
+__device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                uint32_t tries)
+{
+    for (uint32_t it = 0; it < tries; it++) {
+        if (mbar_try(bar, parity, 20000u))
+            return true;
+        if (*abort_flag)
+            return false;
+    }
+    return false;
+}
+
+// shared-memory matrix descriptor (no swizzle): start address, leading (K)
+// and stride (M/N) byte offsets in 16-byte units, version bits of tcgen05
+__device__ __forceinline__ uint64_t mma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.u32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                 "l"(da), "l"(db), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+// instruction descriptor of kind::f16: F32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t mma_idesc(uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+constexpr int kMmaThreads = 192;     // warp 0 copies, warp 1 MMA, warps 2-5 drain
+constexpr uint32_t kMmaTailPad = 2048; // 16 row groups x 128 bytes
+constexpr uint32_t kAccStride = 256; // tensor-memory columns between the two accumulators
+constexpr uint32_t kMmaTmemCols = 512;
+
+} // namespace
+
+// ============================================================================
+__global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w, unsigned* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const unsigned kge = w.kg + (w.kg & 1u);             // K groups the MMAs read (an odd count gets a zero group)
+    const uint32_t a_bytes = kge * w.rga * 128u;         // one of A_hi / A_lo in a stage
+    const uint32_t b_bytes = kge * w.rgb * 128u;         // one of B_hi / B_lo
+    const uint32_t stage_bytes = 2u * (a_bytes + b_bytes);
+    const uint32_t a_copy = w.kg * w.rga * 128u, b_copy = w.kg * w.rgb * 128u; // bytes copied per part
+    // the barriers sit behind kMmaTailPad bytes: an M = 128 MMA reads 16 row
+    // groups of A whatever the tile stores, and the rows beyond a short tile
+    // (never drained) may run past the last stage
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + (size_t)w.n_stages * stage_bytes + kMmaTailPad);
+    uint64_t* full = bars;                  // [n_stages] operands landed
+    uint64_t* empty = bars + w.n_stages;    // [n_stages] MMAs done with the stage
+    uint64_t* accf = empty + w.n_stages;    // [2] accumulator written
+    uint64_t* acce = accf + 2;              // [2] accumulator drained
+    uint64_t* done = acce + 2;              // last MMAs finished (abort path)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (blockIdx.x >= w.n_items)
+        return;
+    const uint32_t wlim = wait_tries(w.wait_iters);
+
+    // the zero K group of an odd K-group count, in every part of every stage
+    if (kge != w.kg) {
+        for (unsigned st = 0; st < w.n_stages; st++) {
+            unsigned char* sb = smem_raw + (size_t)st * stage_bytes;
+            const uint32_t offs[4] = {a_copy, a_bytes + a_copy, 2 * a_bytes + b_copy, 2 * a_bytes + b_bytes + b_copy};
+            const uint32_t lens[4] = {w.rga * 128u, w.rga * 128u, w.rgb * 128u, w.rgb * 128u};
+            for (int part = 0; part < 4; part++)
+                for (uint32_t i = tid * 16; i < lens[part]; i += kMmaThreads * 16)
+                    *reinterpret_cast<uint4*>(sb + offs[part] + i) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    if (warp == 1)
+        tmem_alloc(tmem_slot, kMmaTmemCols);
+    if (tid == 0) {
+        for (unsigned i = 0; i < w.n_stages; i++) {
+            mbar_init(full + i, 1);
+            mbar_init(empty + i, 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(accf + i, 1);
+            mbar_init(acce + i, 128);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    fence_proxy_async(); // the zero groups become visible to the tensor cores
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    bool failed = false;
+    if (warp == 0) {
+        // ================= operand copies =================
+        if (lane == 0) {
+            uint32_t it = 0;
+            for (unsigned item = blockIdx.x; item < w.n_items && !failed; item += gridDim.x) {
+                const unsigned t = item % w.n_rtiles, pb = item / w.n_rtiles; // pb = particle * n_blocks + block
+                const unsigned char* a_src = w.sop + (size_t)pb * kSlots * w.sop_slot;
+                const unsigned char* b_src = w.rop + (size_t)t * kSlots * w.rop_slot;
+                for (unsigned k = 0; k < (unsigned)kSlots; k++, it++) {
+                    const uint32_t st = it % w.n_stages;
+                    if (it >= w.n_stages && !mbar_wait_abort(empty + st, ((it / w.n_stages) - 1u) & 1u, abort_flag, wlim)) {
+                        failed = true;
+                        break;
+                    }
+                    if (w.test_stall)
+                        continue; // failure-path test: no copies
+                    unsigned char* sb = smem_raw + (size_t)st * stage_bytes;
+                    mbar_expect_tx(full + st, 2u * (a_copy + b_copy));
+                    const unsigned char* as = a_src + (size_t)k * w.sop_slot;
+                    const unsigned char* bs = b_src + (size_t)k * w.rop_slot;
+                    bulk_g2s(sb, as, a_copy, full + st);
+                    bulk_g2s(sb + a_bytes, as + a_copy, a_copy, full + st);
+                    bulk_g2s(sb + 2 * a_bytes, bs, b_copy, full + st);
+                    bulk_g2s(sb + 2 * a_bytes + b_bytes, bs + b_copy, b_copy, full + st);
+                }
+            }
+            if (failed) {
+                *abort_flag = 1;
+                atomicExch(err, 1u);
+            }
+            // every issued copy has landed before the CTA ends: the last
+            // n_stages stages' full phases (bounded; on the normal path the
+            // MMA thread has already waited for them)
+            const uint32_t issued = w.test_stall ? 0u : it;
+            for (uint32_t j = issued > w.n_stages ? issued - w.n_stages : 0; j < issued; j++)
+                mbar_wait(full + (j % w.n_stages), (j / w.n_stages) & 1u, wlim);
+        }
+    } else if (warp == 1) {
+        // ================= MMA issue =================
+        if (lane == 0) {
+            const uint32_t idesc = mma_idesc(w.n_cols);
+            const uint32_t ks = kge / 2; // K steps of 16 rings
+            uint32_t it = 0;
+            bool any = false;
+            for (unsigned item = blockIdx.x; item < w.n_items && !failed; item += gridDim.x) {
+                for (unsigned k = 0; k < (unsigned)kSlots; k++, it++) {
+                    const uint32_t st = it % w.n_stages, buf = it & 1u;
+                    if (!mbar_wait_abort(full + st, (it / w.n_stages) & 1u, abort_flag, wlim) ||
+                        (it >= 2 && !mbar_wait_abort(acce + buf, ((it >> 1) - 1u) & 1u, abort_flag, wlim))) {
+                        failed = true;
+                        break;
+                    }
+                    tmem_fence_after();
+                    const uint32_t sa = smem_addr(smem_raw + (size_t)st * stage_bytes);
+                    const uint32_t sa_lo = sa + a_bytes, sb_hi = sa + 2 * a_bytes, sb_lo = sb_hi + b_bytes;
+                    const uint32_t d = tmem + buf * kAccStride;
+                    const uint32_t lbo_a = w.rga * 128u, lbo_b = w.rgb * 128u;
+#pragma unroll 1
+                    for (uint32_t j = 0; j < ks; j++) {
+                        const uint32_t oa = 2 * j * lbo_a, ob = 2 * j * lbo_b;
+                        const uint64_t ah = mma_desc(sa + oa, lbo_a, 128), al = mma_desc(sa_lo + oa, lbo_a, 128);
+                        const uint64_t bh = mma_desc(sb_hi + ob, lbo_b, 128), bl = mma_desc(sb_lo + ob, lbo_b, 128);
+                        mma_bf16(d, ah, bh, idesc, j > 0 ? 1u : 0u);
+                        mma_bf16(d, ah, bl, idesc, 1u);
+                        mma_bf16(d, al, bh, idesc, 1u);
+                    }
+                    mma_commit(empty + st);
+                    mma_commit(accf + buf);
+                    any = true;
+                }
+            }
+            if (failed) {
+                *abort_flag = 1;
+                atomicExch(err, 1u);
+                if (any) { // the MMAs already issued finish before the tensor memory is freed
+                    mma_commit(done);
+                    mbar_wait(done, 0, wlim);
+                }
+            }
+        }
+    } else {
+        // ================= drain: accumulators -> Z =================
+        const int quad = warp & 3;              // tensor-memory lanes 32 quad .. 32 quad + 31
+        const unsigned row = 32 * quad + lane;  // operand row = 2 shift + {0: a, 1: b}
+        const unsigned sl = row >> 1;           // shift within the block
+        const bool is_b = row & 1u;
+        uint32_t it = 0;
+        for (unsigned item = blockIdx.x; item < w.n_items && !failed; item += gridDim.x) {
+            const unsigned t = item % w.n_rtiles, pb = item / w.n_rtiles;
+            const unsigned p = pb / w.n_blocks, b = pb - p * w.n_blocks;
+            const unsigned q0 = t * w.rblock, nq = min(w.rblock, w.n_ref - q0);
+            const unsigned s0 = b * w.block, nsb = min(w.block, w.n_shift - s0);
+            const bool row_ok = sl < nsb;
+            // Z of (p, q, b): [256][zw] float2, shift fastest
+            float2* zbase = w.z + ((size_t)(p * w.n_ref + q0) * w.n_blocks + b) * kRingLen * w.zw + sl;
+            const size_t zq = (size_t)w.n_blocks * kRingLen * w.zw; // between references
+            const unsigned nchunk = (2 * nq + 15) / 16;
+            for (unsigned k = 0; k < (unsigned)kSlots; k++, it++) {
+                const uint32_t buf = it & 1u;
+                const bool ok = mbar_wait_abort(accf + buf, (it >> 1) & 1u, abort_flag, wlim);
+                if (!__all_sync(0xffffffffu, ok)) {
+                    failed = true;
+                    break;
+                }
+                tmem_fence_after();
+                const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + buf * kAccStride;
+                // Z[k] (a rows) and Z[256 - k] (b rows); slot 0: Z[0], Z[128]
+                const size_t zoff = (size_t)(is_b ? (k ? kRingLen - k : kSlots) : k) * w.zw;
+                for (unsigned c = 0; c < nchunk; c++) {
+                    float r[16];
+                    tmem_ld16_async(taddr + 16 * c, r);
+                    tmem_wait_ld16(r);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const float u = r[2 * j], v = r[2 * j + 1];
+                        const float pu = __shfl_xor_sync(0xffffffffu, u, 1);
+                        const float pv = __shfl_xor_sync(0xffffffffu, v, 1);
+                        // a row: u = sum u a, v = sum v a; b row: u = sum u b, v = sum v b
+                        const float a1 = is_b ? pu : u, a4 = is_b ? pv : v;
+                        const float a2 = is_b ? u : pu, a3 = is_b ? v : pv;
+                        const unsigned ql = 8 * c + j;
+                        if (row_ok && ql < nq) {
+                            float2 zv;
+                            if (k == 0) {
+                                const float p1 = 0.25f * (a1 + a2 + a3 + a4);
+                                const float p2 = 0.25f * (a1 - a2 + a3 - a4);
+                                zv = is_b ? make_float2(p2, p2) : make_float2(p1, p1);
+                            } else {
+                                zv = is_b ? make_float2(a3, a4) : make_float2(a1, a2);
+                            }
+                            zbase[ql * zq + zoff] = zv;
+                        }
+                    }
+                }
+                tmem_fence_before();
+                mbar_arrive(acce + buf);
+            }
+        }
+        if (failed && lane == 0) {
+            *abort_flag = 1;
+            atomicExch(err, 1u);
+        }
+    }
+    // release the tensor memory (all tcgen05 accesses of the CTA are done)
+    tmem_fence_before();
+    __syncthreads();
+    tmem_fence_after();
+    if (warp == 1)
+        tmem_dealloc(tmem, kMmaTmemCols);
+}
+
+// ============================================================================
+// inverse FFT + peak search of the pair spectra Z, one (particle, reference)
+// per work item; RR shifts per 16-thread group and shift block
+template <int RR>
+__global__ void __launch_bounds__(512, 1)
+zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const unsigned groups = blockDim.x >> 4;
+    const size_t zbuf_bytes = std::max((size_t)kRingLen * w.zw * sizeof(float2),
+                                       (size_t)groups * kPairStride * sizeof(float2));
+    float2* const zb0 = reinterpret_cast<float2*>(smem_raw);
+    float2* const zb1 = reinterpret_cast<float2*>(smem_raw + zbuf_bytes);
+    float2* tw = reinterpret_cast<float2*>(smem_raw + 2 * zbuf_bytes); // [16][kTwRow]
+    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);    // [groups]
+    uint64_t* full = reinterpret_cast<uint64_t*>(slots + 32);          // [2]
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 2);
+
+    const int tid = threadIdx.x;
+    const unsigned n_items = w.n_part * w.n_ref;
+    if (blockIdx.x >= n_items)
+        return;
+    for (int i = tid; i < kRingLen; i += blockDim.x) { // lane l's inverse-FFT twiddles, row l
+        const int tl = i >> 4, tj = i & 15;
+        const float2 t = twiddle[(tl * tj) & (kRingLen - 1)];
+        tw[tl * kTwRow + tj] = make_float2(t.x, t.y * -1.f);
+    }
+    if (tid == 0) {
+        mbar_init(full, 1);
+        mbar_init(full + 1, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    const size_t unit_elems = (size_t)kRingLen * w.zw;
+    // units of this CTA: (item, block), item = particle x reference
+    const unsigned my_items = (n_items - blockIdx.x + gridDim.x - 1) / gridDim.x;
+    const unsigned n_units = my_items * w.n_blocks;
+    auto unit_item = [&](unsigned u) { return blockIdx.x + (u / w.n_blocks) * gridDim.x; };
+    const uint32_t wlim = wait_tries(w.wait_iters);
+    auto issue = [&](unsigned u) {
+        if (w.test_stall)
+            return; // failure-path test: no copies
+        const unsigned item = unit_item(u), b = u % w.n_blocks;
+        const uint32_t bytes = (uint32_t)(unit_elems * sizeof(float2));
+        fence_proxy_async();
+        mbar_expect_tx(full + (u & 1u), bytes);
+        bulk_g2s((u & 1u) ? zb1 : zb0, w.z + ((size_t)item * w.n_blocks + b) * unit_elems, bytes, full + (u & 1u));
+    };
+    if (tid == 0) {
+        issue(0);
+        if (n_units > 1)
+            issue(1);
+    }
+
+    const int g = tid >> 4, l = tid & 15;
+    const unsigned gmask = 0xffffu << (tid & 16);
+    PeakState st;
+    st.reset(w.rule);
+    bool failed = false;
+    unsigned u = 0;
+    for (; u < n_units; u++) {
+        const unsigned buf = u & 1u, item = unit_item(u), b = u % w.n_blocks;
+        const unsigned s0 = b * w.block, nsb = min(w.block, w.n_shift - s0);
+        const bool ok = mbar_wait(full + buf, (u >> 1) & 1u, wlim);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        float2* const zcur = buf ? zb1 : zb0;
+        // this group's shift columns into registers
+        float2 x[RR][16];
+#pragma unroll
+        for (int rr = 0; rr < RR; rr++) {
+            const unsigned sl = g + rr * groups;
+            if (sl < nsb) {
+#pragma unroll
+                for (int m = 0; m < 16; m++)
+                    x[rr][m] = zcur[(l + 16 * m) * w.zw + sl];
+            }
+        }
+        __syncthreads(); // the buffer now serves as the groups' FFT workspaces
+        float2* gz = zcur + g * kPairStride;
+#pragma unroll
+        for (int rr = 0; rr < RR; rr++) {
+            const unsigned sl = g + rr * groups;
+            if (sl < nsb) // group-uniform
+                fft_peak_regs<true>(x[rr], gz, tw + l * kTwRow, l, gmask, s0 + sl, w.n_shift, st, w.rule);
+        }
+        if (b == w.n_blocks - 1) {
+            // every shift of the pair has been searched: merge the groups
+            park_slot(slots, st, g, l);
+            __syncthreads();
+            if (tid == 0) {
+                unsigned best = 0;
+                for (unsigned i = 1; i < groups; i++)
+                    if (better(slots[i].v, slots[i].h, slots[i].t, slots[best].v, slots[best].h, slots[best].t))
+                        best = i;
+                const PeakSlot& ps = slots[best];
+                const bool mirror = ps.h >= w.n_shift;
+                const unsigned sidx = mirror ? ps.h - w.n_shift : ps.h;
+                const float angle =
+                    w.rule == kPeakPreAlign ? pre_peak_angle(ps.nb, ps.t, mirror) : peak_angle(ps.nb, ps.t, mirror);
+                const unsigned p = item / w.n_ref, q = item - p * w.n_ref;
+                const unsigned pg = w.p_first + p;
+                const float bx = w.base ? w.base[pg].x : 0.f, by = w.base ? w.base[pg].y : 0.f;
+                const float2 sf = w.shifts_f[sidx];
+                const size_t o = (size_t)q * w.p_total + pg;
+                w.d_out[o] = ps.v;
+                w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+            }
+            st.reset(w.rule);
+        }
+        __syncthreads(); // buffer and slots free
+        if (tid == 0 && u + 2 < n_units)
+            issue(u + 2);
+    }
+    if (failed && tid == 0) {
+        atomicExch(err, 1u);
+        // copies in flight land before the CTA ends (bounded)
+        for (unsigned v = u; v < std::min(u + 2, n_units) && !w.test_stall; v++)
+            mbar_wait(full + (v & 1u), (v >> 1) & 1u, wlim);
+    }
+}
+
+// ============================================================================
+
+static int device_sms()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(sms, 1);
+}
+
+
+static size_t mma_stage_bytes(const SplitPlan& p)
+{
+    const unsigned kge = p.kg + (p.kg & 1u);
+    return (size_t)2 * kge * (p.rga + p.rgb) * 128;
+}
+
+static size_t mma_smem(const SplitPlan& p) { return (size_t)p.n_stages * mma_stage_bytes(p) + kMmaTailPad + 256; }
+
+static size_t fft_smem(const SplitPlan& p)
+{
+    const size_t zbuf = std::max((size_t)kRingLen * p.zw * sizeof(float2), (size_t)p.fft_groups * kPairStride * sizeof(float2));
+    return 2 * zbuf + 16 * kTwRow * sizeof(float2) + 32 * sizeof(PeakSlot) + 64;
+}
+
+bool split_plan(unsigned ring_num, unsigned n_shift, unsigned n_ref, SplitPlan& p)
+{
+    if (ring_num == 0 || ring_num > kMaxRingNum || n_shift == 0 || n_ref == 0)
+        return false;
+    p.n_blocks = (n_shift + kSplitMaxBlock - 1) / kSplitMaxBlock;
+    p.block = (n_shift + p.n_blocks - 1) / p.n_blocks;
+    p.zw = p.block | 1u; // odd row length: the FFT's column reads hit distinct banks
+    p.kg = (ring_num + 7) / 8;
+    p.rga = (2 * p.block + 7) / 8;
+    p.rounds = p.block > 32 ? 2 : 1;
+    p.fft_groups = (p.block + p.rounds - 1) / p.rounds;
+    const size_t cap = std::min<size_t>((size_t)smem_optin_max(), 227 * 1024);
+    // references per tile: as many as N = 2 x refs <= 256 allows with at
+    // least two operand stages, tiles balanced
+    for (unsigned maxq = 128; maxq >= 8; maxq /= 2) {
+        const unsigned tiles = (n_ref + maxq - 1) / maxq;
+        p.rblock = (n_ref + tiles - 1) / tiles;
+        p.n_rtiles = (n_ref + p.rblock - 1) / p.rblock;
+        p.n_cols = (2 * p.rblock + 15) / 16 * 16;
+        p.rgb = p.n_cols / 8;
+        p.n_stages = 0;
+        const size_t sb = mma_stage_bytes(p);
+        const unsigned fit = (unsigned)std::min<size_t>(4, (cap - kMmaTailPad - 256) / sb);
+        if (fit >= 2) {
+            p.n_stages = fit;
+            break;
+        }
+    }
+    if (p.n_stages < 2 || fft_smem(p) > cap)
+        return false;
+    p.sop_slot = (size_t)2 * p.kg * p.rga * 128;
+    p.rop_slot = (size_t)2 * p.kg * p.rgb * 128;
+    return true;
+}
+
+size_t split_sop_bytes(const SplitPlan& p, unsigned n_part) { return (size_t)n_part * p.n_blocks * kSlots * p.sop_slot; }
+size_t split_rop_bytes(const SplitPlan& p) { return (size_t)p.n_rtiles * kSlots * p.rop_slot; }
+size_t split_z_bytes(const SplitPlan& p, unsigned n_part, unsigned n_ref)
+{
+    return (size_t)n_part * n_ref * p.n_blocks * kRingLen * p.zw * sizeof(float2);
+}
+
+OperandLayout split_sbj_layout(const SplitPlan& p, unsigned char* base)
+{
+    OperandLayout o;
+    o.base = base;
+    o.kg = p.kg;
+    o.rg = p.rga;
+    o.block = p.block;
+    o.n_blocks = p.n_blocks;
+    return o;
+}
+
+OperandLayout split_ref_layout(const SplitPlan& p, unsigned char* base)
+{
+    OperandLayout o;
+    o.base = base;
+    o.kg = p.kg;
+    o.rg = p.rgb;
+    o.block = p.rblock;
+    o.n_blocks = 1;
+    return o;
+}
+
+cudaError_t launch_ccf_mma(const SplitPlan& p, const unsigned char* sop, const unsigned char* rop, float2* z,
+                           unsigned n_part, unsigned n_ref, unsigned n_shift, unsigned* err, cudaStream_t stream)
+{
+    if (n_part == 0 || n_ref == 0)
+        return cudaSuccess;
+    SplitMmaWork mw;
+    mw.sop = sop;
+    mw.rop = rop;
+    mw.z = z;
+    mw.n_part = n_part;
+    mw.n_blocks = p.n_blocks;
+    mw.block = p.block;
+    mw.n_shift = n_shift;
+    mw.n_ref = n_ref;
+    mw.rblock = p.rblock;
+    mw.n_rtiles = p.n_rtiles;
+    mw.kg = p.kg;
+    mw.rga = p.rga;
+    mw.rgb = p.rgb;
+    mw.n_cols = p.n_cols;
+    mw.n_stages = p.n_stages;
+    mw.zw = p.zw;
+    mw.sop_slot = p.sop_slot;
+    mw.rop_slot = p.rop_slot;
+    mw.n_items = n_part * p.n_blocks * p.n_rtiles;
+    ccf_test_settings(mw.test_stall, mw.wait_iters);
+    const size_t ms = mma_smem(p);
+    cudaError_t e = opt_in_smem_k(ccf_mma_kernel, ms);
+    if (e != cudaSuccess)
+        return e;
+    ccf_mma_kernel<<<std::min<unsigned>(mw.n_items, device_sms()), kMmaThreads, ms, stream>>>(mw, err);
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zfft_peak(const SplitPlan& p, const float2* z, unsigned n_part, unsigned p_first,
+                             unsigned p_total, unsigned n_ref, unsigned n_shift, const float2* twiddle,
+                             const float2* shifts_f, const float2* base, float* d_out, float4* peak_out,
+                             unsigned* err, cudaStream_t stream, unsigned rule)
+{
+    if (n_part == 0 || n_ref == 0)
+        return cudaSuccess;
+    SplitFftWork fw;
+    fw.z = z;
+    fw.n_part = n_part;
+    fw.n_ref = n_ref;
+    fw.n_shift = n_shift;
+    fw.n_blocks = p.n_blocks;
+    fw.block = p.block;
+    fw.zw = p.zw;
+    fw.p_first = p_first;
+    fw.p_total = p_total;
+    fw.shifts_f = shifts_f;
+    fw.base = base;
+    fw.d_out = d_out;
+    fw.peak_out = peak_out;
+    fw.rule = rule;
+    ccf_test_settings(fw.test_stall, fw.wait_iters);
+    const size_t fs = fft_smem(p);
+    const unsigned grid = std::min<unsigned>(n_part * n_ref, device_sms());
+    cudaError_t e;
+    if (p.rounds == 1) {
+        if ((e = opt_in_smem_k(zfft_peak_kernel<1>, fs)) != cudaSuccess)
+            return e;
+        zfft_peak_kernel<1><<<grid, 16 * p.fft_groups, fs, stream>>>(fw, twiddle, err);
+    } else {
+        if ((e = opt_in_smem_k(zfft_peak_kernel<2>, fs)) != cudaSuccess)
+            return e;
+        zfft_peak_kernel<2><<<grid, 16 * p.fft_groups, fs, stream>>>(fw, twiddle, err);
+    }
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+} // namespace gpuisac

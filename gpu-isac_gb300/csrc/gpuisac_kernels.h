@@ -32,6 +32,18 @@ size_t ccf_peak_smem_bytes(unsigned ring_num);
 // kernels launched by this library since load (all launchers count here)
 extern std::atomic<unsigned long long> g_kernel_launches;
 
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) applies to the current
+// device only: opt `kernel` in to at least `bytes` of dynamic shared memory
+// on the current device, once per (device, kernel, larger size); thread-safe
+cudaError_t opt_in_smem(const void* kernel, int bytes);
+template <typename K>
+inline cudaError_t opt_in_smem_k(K* kernel, size_t bytes)
+{
+    return opt_in_smem(reinterpret_cast<const void*>(kernel), (int)bytes);
+}
+// the device's opt-in maximum per block (current device)
+int smem_optin_max();
+
 // A device stack laid out as the reference's textures hold it (batches of
 // st.batch images in textures of st.tex images, stale slots of a short final
 // batch filled from the previous batch), one texture object per segment
@@ -74,6 +86,41 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
                                  float2* out, cudaStream_t stream, const unsigned* img_list = nullptr,
                                  const unsigned long long* tex_objs = nullptr);
 
+// ---------------------------------------------------------------------------
+// Operands of the tensor-core contraction (ccf_split.cu).  For every spectrum
+// slot k the contraction is a GEMM over the rings: subject rows (one image
+// row = particle x shift, two operand rows: the a and b parts of its spectra)
+// against reference rows (one reference, two operand rows: u and v), with
+// each FP32 value split into a BF16 high part and the BF16 rounding of the
+// remainder.  A tile's operand for slot k is, in bytes,
+//   [hl: hi, lo][kg: group of 8 rings][rg: group of 8 operand rows][8 rows][8 rings x 2 B]
+// -- the canonical no-swizzle K-major layout of tcgen05 with 128-byte core
+// matrices, K groups kg_stored = ceil(rings / 8) (rings beyond the count
+// hold zero), rg row groups per tile.
+//   subjects: tile = (particle, shift block), shift s of block b = s / block
+//             at rows 2 (s % block) + {0: a, 1: b};
+//   references: tile = block consecutive references, reference q at rows
+//             2 (q % block) + {0: u, 1: v}, the ring weight (r+1) folded in.
+struct OperandLayout {
+    unsigned char* base = nullptr; // [tiles][kSlots][slot_bytes()]
+    unsigned kg = 0;               // K groups stored
+    unsigned rg = 0;               // row groups per tile
+    unsigned block = 0;            // image rows per tile: shifts (subjects) or references
+    unsigned n_blocks = 1;         // subjects: shift blocks per particle
+    __host__ __device__ size_t slot_bytes() const { return (size_t)2 * kg * rg * 128; }
+    __host__ __device__ size_t tile_bytes() const { return slot_bytes() * kSlots; }
+};
+
+// The same resampling and FFT, written as tensor-core operands (opnd.base
+// set): subjects (is_ref = 0) as rows of particle tiles, references (is_ref)
+// as rows of reference tiles; the spectra values are those
+// launch_polar_spectra writes, bit for bit, before the split.
+cudaError_t launch_polar_operands(const StackDesc& st, const float2* tmpl, const float2* twiddle,
+                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,
+                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
+                                  const OperandLayout& opnd, cudaStream_t stream,
+                                  const unsigned long long* tex_objs = nullptr);
+
 // CCF against every reference + inverse FFT + peak search for n_part particles
 // whose spectra are in sbj_sp ([n_part][n_shift][ring_num][kSlots]); results
 // for particle i go to column p_global0 + i of d_out [n_ref][p_total] and
@@ -112,7 +159,15 @@ struct CcfWork {
     unsigned n_items;
     unsigned ppc;     // particles per work item
     unsigned max_ref; // most references of any group (0: not known); 1 selects the one-reference contraction
+    // failure-path tests only (gpuisac_test_stall_ccf): the kernels that stage
+    // with bulk copies issue none, and their bounded waits give up after
+    // wait_iters tries (0: the default, about a second)
+    unsigned test_stall;
+    unsigned wait_iters;
 };
+
+// the failure-path test settings every CCF launch carries (both 0 normally)
+void ccf_test_settings(unsigned& stall, unsigned& wait_iters);
 
 enum { kCcfGeneral = 0, kCcfTmem = 1, kCcfWs = 2 };
 constexpr unsigned kCcfParticlesPerItem = 8;

@@ -57,6 +57,39 @@ int fail(int code, const char* msg)
 
 } // namespace
 
+namespace {
+
+// the array carved for one call: tables, reference spectra, then as many
+// particles' spectra as fit
+struct Carve {
+    size_t off_err, off_tw, off_zero, off_tmpl, off_sf, off_si, off_ref, off_sbj, per_particle, need;
+    unsigned chunk;
+};
+
+Carve carve(const HostGeometry& g)
+{
+    Carve c;
+    const size_t row_bytes = (size_t)g.NR * kSlots * sizeof(float2); // one (image, shift) row
+    c.off_err = 0;
+    c.off_tw = c.off_err + 256;
+    c.off_zero = c.off_tw + up256(kRingLen * sizeof(float2));
+    c.off_tmpl = c.off_zero + up256(sizeof(int2));
+    c.off_sf = c.off_tmpl + up256(g.tmpl.size() * sizeof(float2));
+    c.off_si = c.off_sf + up256((size_t)g.S * sizeof(float2));
+    c.off_ref = c.off_si + up256((size_t)g.S * sizeof(int2));
+    c.off_sbj = c.off_ref + up256((size_t)g.R * row_bytes);
+    c.per_particle = (size_t)g.S * row_bytes;
+    c.need = c.off_sbj + c.per_particle;
+    c.chunk = c.need > kNoAllocScratchBytes
+                  ? 0u
+                  : (unsigned)std::min<size_t>((kNoAllocScratchBytes - c.off_sbj) / c.per_particle, g.P);
+    return c;
+}
+
+int enqueue_and_wait(const HostGeometry& g, const Carve& c, unsigned char* base, cudaStream_t st, const float* sbj,
+                     const float* ref, const float* base_shift, float* d_out, float* peak_out, int dev);
+} // namespace
+
 extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, const float* sbj, const float* ref,
                                                       const float* base_shift, float* d_out, float* peak_out,
                                                       void* stream)
@@ -70,27 +103,15 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
     if (g.P == 0 || g.R == 0)
         return 0;
 
-    // carve the array: tables, reference spectra, then as many particles'
-    // spectra as fit
-    const size_t row_bytes = (size_t)g.NR * kSlots * sizeof(float2); // one (image, shift) row
-    const size_t off_err = 0;
-    const size_t off_tw = off_err + 256;
-    const size_t off_zero = off_tw + up256(kRingLen * sizeof(float2));
-    const size_t off_tmpl = off_zero + up256(sizeof(int2));
-    const size_t off_sf = off_tmpl + up256(g.tmpl.size() * sizeof(float2));
-    const size_t off_si = off_sf + up256((size_t)g.S * sizeof(float2));
-    const size_t off_ref = off_si + up256((size_t)g.S * sizeof(int2));
-    const size_t off_sbj = off_ref + up256((size_t)g.R * row_bytes);
-    const size_t per_particle = (size_t)g.S * row_bytes;
-    if (off_sbj + per_particle > kNoAllocScratchBytes) {
+    const Carve c = carve(g);
+    if (c.chunk == 0) {
         char m[320];
         snprintf(m, sizeof(m),
                  "workload needs %zu bytes of work space (reference spectra + one particle's spectra); the "
                  "allocation-free entry point has %zu: use gpuisac_multi_ref_align_device",
-                 off_sbj + per_particle, kNoAllocScratchBytes);
+                 c.need, kNoAllocScratchBytes);
         return fail(2, m);
     }
-    const unsigned chunk = (unsigned)std::min<size_t>((kNoAllocScratchBytes - off_sbj) / per_particle, g.P);
 
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     int dev = 0;
@@ -106,16 +127,35 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
         g_noalloc_dev[dev] = static_cast<unsigned char*>(p);
     }
     unsigned char* base = g_noalloc_dev[dev];
-    unsigned* err = reinterpret_cast<unsigned*>(base + off_err);
-    float2* tw = reinterpret_cast<float2*>(base + off_tw);
-    int2* zero = reinterpret_cast<int2*>(base + off_zero);
-    float2* tmpl = reinterpret_cast<float2*>(base + off_tmpl);
-    float2* sf = reinterpret_cast<float2*>(base + off_sf);
-    int2* si = reinterpret_cast<int2*>(base + off_si);
-    float2* ref_sp = reinterpret_cast<float2*>(base + off_ref);
-    float2* sbj_sp = reinterpret_cast<float2*>(base + off_sbj);
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // From the first enqueue on, work on `st` reads and writes the shared
+    // array: a failure returns only after that work has finished, so that
+    // the next caller (another stream, once the lock is released) cannot
+    // overwrite the array under it.
+    const int rc2 = enqueue_and_wait(g, c, base, st, sbj, ref, base_shift, d_out, peak_out, dev);
+    if (rc2)
+        cudaStreamSynchronize(st); // its own error, if any, is already recorded
+    return rc2;
+}
+
+namespace {
+
+// enqueue the whole alignment on st and wait for it (the host tables and the
+// shared array must outlive the work)
+int enqueue_and_wait(const HostGeometry& g, const Carve& c, unsigned char* base, cudaStream_t st, const float* sbj,
+                     const float* ref, const float* base_shift, float* d_out, float* peak_out, int dev)
+{
+    const unsigned chunk = c.chunk;
+    unsigned* err = reinterpret_cast<unsigned*>(base + c.off_err);
+    float2* tw = reinterpret_cast<float2*>(base + c.off_tw);
+    int2* zero = reinterpret_cast<int2*>(base + c.off_zero);
+    float2* tmpl = reinterpret_cast<float2*>(base + c.off_tmpl);
+    float2* sf = reinterpret_cast<float2*>(base + c.off_sf);
+    int2* si = reinterpret_cast<int2*>(base + c.off_si);
+    float2* ref_sp = reinterpret_cast<float2*>(base + c.off_ref);
+    float2* sbj_sp = reinterpret_cast<float2*>(base + c.off_sbj);
+
     const int2 zero_h = make_int2(0, 0);
     NA_CK(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
     NA_CK(cudaMemcpyAsync(tw, g.tw.data(), kRingLen * sizeof(float2), cudaMemcpyHostToDevice, st));
@@ -138,7 +178,6 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
         NA_CK(launch_ccf_peak(sbj_sp, ref_sp, tw, g.NR, g.S, g.R, n, p0, g.P, sf, bs, d_out,
                               reinterpret_cast<float4*>(peak_out), err, st));
     }
-    // the host tables and the shared array must outlive the work
     NA_CK(cudaStreamSynchronize(st));
     unsigned flag = 0;
     NA_CK(cudaMemcpy(&flag, err, sizeof(unsigned), cudaMemcpyDeviceToHost));
@@ -146,3 +185,5 @@ extern "C" int gpuisac_multi_ref_align_device_noalloc(const AlignConfig* cfg, co
         return fail(1, "a kernel timed out waiting for its own asynchronous copies");
     return 0;
 }
+
+} // namespace

@@ -13,6 +13,12 @@
 // are exactly Re/Im of Z[k] = O[k] + i M[k] and of Z[256-k], the spectrum
 // whose inverse FFT gives the normal (real part) and mirrored (imaginary
 // part) correlation at once.
+#include <cuda_bf16.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "gpuisac_device.cuh"
 #include "gpuisac_kernels.h"
 
@@ -20,15 +26,56 @@ namespace gpuisac {
 
 std::atomic<unsigned long long> g_kernel_launches{0};
 
+namespace {
+std::mutex g_optin_mu;
+std::map<std::pair<int, const void*>, int> g_optin; // (device, kernel) -> bytes opted in
+} // namespace
+
+cudaError_t opt_in_smem(const void* kernel, int bytes)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    std::lock_guard<std::mutex> lk(g_optin_mu);
+    auto it = g_optin.find({dev, kernel});
+    if (it != g_optin.end() && it->second >= bytes)
+        return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        g_optin[{dev, kernel}] = bytes;
+    return e;
+}
+
+int smem_optin_max()
+{
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
 // smem offset (floats) of ring r's samples
 __device__ __forceinline__ unsigned polar_index(unsigned r) { return (r >> 1) * 2 * kPairStride + (r & 1) * kRingLen; }
 
-__global__ void __launch_bounds__(256, 5)
-polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
-                     unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
-                     const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
-                     float2* __restrict__ out, const unsigned* __restrict__ img_list,
-                     const unsigned long long* __restrict__ tex_objs)
+// split x into BF16 hi = rn(x) and lo = rn(x - hi) (x - hi is exact in FP32)
+__device__ __forceinline__ void bf16_split(float x, uint32_t& hi, uint32_t& lo)
+{
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+    hi = (uint32_t)__bfloat16_as_ushort(h);
+    lo = (uint32_t)__bfloat16_as_ushort(l);
+}
+
+// kOperand: the spectra go to shared memory and leave as BF16 hi/lo
+// tensor-core operands (OperandLayout) instead of FP32 rows
+template <bool kOperand>
+__device__ __forceinline__ void
+polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
+                   unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
+                   const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
+                   float2* __restrict__ out, const unsigned* __restrict__ img_list,
+                   const unsigned long long* __restrict__ tex_objs, const OperandLayout& opnd)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // ring pair p's samples at polar[p * 2 * kPairStride + (r & 1) * 256 + angle];
@@ -117,6 +164,7 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
         const float* pa = polar + pr * 2 * kPairStride;
         float2* gws = reinterpret_cast<float2*>(polar) + pr * kPairStride;
         float2 x[16];
+        float2 oa[kOperand ? 8 : 1], ob[kOperand ? 8 : 1];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             float va = (pa[l + 16 * m] - avg_f) * inv_f;
@@ -147,12 +195,84 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
             }
             float wa = is_ref ? (float)(ra + 1) : 1.f;
             float wb = is_ref ? (float)(rb + 1) : 1.f;
-            out_row[ra * kSlots + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
-            if (has_b)
-                out_row[rb * kSlots + k] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
+            if (kOperand) {
+                oa[i] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
+                ob[i] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
+            } else {
+                out_row[ra * kSlots + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
+                if (has_b)
+                    out_row[rb * kSlots + k] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
+            }
         }
         __syncwarp(gmask);
+        if (kOperand) {
+            // the pair's region now holds its two rings' spectra: ring ra at
+            // [0, 128), ring rb at [128, 256) (zero for a missing ring)
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                gws[l + 16 * i] = oa[i];
+                gws[kSlots + l + 16 * i] = has_b ? ob[i] : make_float2(0.f, 0.f);
+            }
+            __syncwarp(gmask);
+        }
     }
+    if (!kOperand)
+        return;
+    __syncthreads();
+    // ---- write-out as BF16 hi/lo operand rows ----
+    const unsigned tile = is_ref ? img_local / opnd.block : img_local * opnd.n_blocks + s / opnd.block;
+    const unsigned orow = 2 * (is_ref ? img_local % opnd.block : s % opnd.block); // a / u; +1: b / v
+    unsigned char* tb = opnd.base + (size_t)tile * opnd.tile_bytes() + (orow >> 3) * 128 + (orow & 7) * 16;
+    const size_t sb = opnd.slot_bytes(), hb = (size_t)opnd.kg * opnd.rg * 128, kb = (size_t)opnd.rg * 128;
+    const float2* spec = reinterpret_cast<const float2*>(polar);
+    for (unsigned it = tid; it < kSlots * opnd.kg; it += 256) {
+        const unsigned k = it & (kSlots - 1), kgi = it >> 7;
+        uint32_t ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float2 v[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const unsigned r = 8 * kgi + 2 * j + h;
+                v[h] = r < ring_num ? spec[(r >> 1) * kPairStride + (r & 1) * kSlots + k] : make_float2(0.f, 0.f);
+            }
+            uint32_t h0, l0, h1, l1;
+            bf16_split(v[0].x, h0, l0);
+            bf16_split(v[1].x, h1, l1);
+            ah[j] = h0 | (h1 << 16);
+            al[j] = l0 | (l1 << 16);
+            bf16_split(v[0].y, h0, l0);
+            bf16_split(v[1].y, h1, l1);
+            bh[j] = h0 | (h1 << 16);
+            bl[j] = l0 | (l1 << 16);
+        }
+        unsigned char* p = tb + k * sb + kgi * kb;
+        *reinterpret_cast<uint4*>(p) = make_uint4(ah[0], ah[1], ah[2], ah[3]);
+        *reinterpret_cast<uint4*>(p + 16) = make_uint4(bh[0], bh[1], bh[2], bh[3]);
+        *reinterpret_cast<uint4*>(p + hb) = make_uint4(al[0], al[1], al[2], al[3]);
+        *reinterpret_cast<uint4*>(p + hb + 16) = make_uint4(bl[0], bl[1], bl[2], bl[3]);
+    }
+}
+
+__global__ void __launch_bounds__(256, 5)
+polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
+                     unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
+                     const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
+                     float2* __restrict__ out, const unsigned* __restrict__ img_list,
+                     const unsigned long long* __restrict__ tex_objs)
+{
+    polar_spectra_body<false>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base, img0, n_img, is_ref, out,
+                              img_list, tex_objs, OperandLayout());
+}
+
+__global__ void __launch_bounds__(256, 4)
+polar_operands_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2* __restrict__ twiddle,
+                      unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
+                      const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
+                      OperandLayout opnd, const unsigned long long* __restrict__ tex_objs)
+{
+    polar_spectra_body<true>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base, img0, n_img, is_ref, nullptr,
+                             nullptr, tex_objs, opnd);
 }
 
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
@@ -164,17 +284,34 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
     if (n_img == 0 || n_shift == 0)
         return cudaSuccess;
     size_t smem = polar_spectra_smem_bytes(ring_num);
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(polar_spectra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)polar_spectra_smem_bytes(kMaxRingNum));
-        if (e != cudaSuccess)
-            return e;
-        configured = true;
-    }
+    cudaError_t e = opt_in_smem_k(polar_spectra_kernel, polar_spectra_smem_bytes(kMaxRingNum));
+    if (e != cudaSuccess)
+        return e;
     unsigned rows = n_img * n_shift;
     polar_spectra_kernel<<<rows, 256, smem, stream>>>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base,
                                                        img0, n_img, is_ref, out, img_list, tex_objs);
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_polar_operands(const StackDesc& st, const float2* tmpl, const float2* twiddle,
+                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,
+                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
+                                  const OperandLayout& opnd, cudaStream_t stream,
+                                  const unsigned long long* tex_objs)
+{
+    if (n_img == 0 || n_shift == 0)
+        return cudaSuccess;
+    if (!opnd.base || opnd.block == 0 || opnd.kg * 8 < ring_num || (is_ref && n_shift != 1) ||
+        opnd.rg * 8 < 2 * opnd.block || (!is_ref && opnd.block * opnd.n_blocks < n_shift))
+        return cudaErrorInvalidValue;
+    size_t smem = polar_spectra_smem_bytes(ring_num);
+    cudaError_t e = opt_in_smem_k(polar_operands_kernel, polar_spectra_smem_bytes(kMaxRingNum));
+    if (e != cudaSuccess)
+        return e;
+    unsigned rows = n_img * n_shift;
+    polar_operands_kernel<<<rows, 256, smem, stream>>>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base, img0,
+                                                        n_img, is_ref, opnd, tex_objs);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

@@ -48,7 +48,7 @@ EXPORTS = (
     "gpuisac_nn_softmax_xent", "gpuisac_nn_adam", "gpuisac_nn_topk", "gpuisac_nn_col_stats",
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
-    "gpuisac_ref_free_averages",
+    "gpuisac_ref_free_averages", "gpuisac_set_contraction", "gpuisac_get_contraction", "gpuisac_test_stall_ccf",
 )
 
 
@@ -180,6 +180,12 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_kernel_time.restype = ctypes.c_int
     L.gpuisac_shift_count.argtypes = [aln_cfg_ptr]
     L.gpuisac_shift_count.restype = ctypes.c_int
+    L.gpuisac_set_contraction.argtypes = [ctypes.c_int]
+    L.gpuisac_set_contraction.restype = ctypes.c_int
+    L.gpuisac_get_contraction.argtypes = []
+    L.gpuisac_get_contraction.restype = ctypes.c_int
+    L.gpuisac_test_stall_ccf.argtypes = [ctypes.c_uint]
+    L.gpuisac_test_stall_ccf.restype = None
     if path is None:
         _lib = L
     return L

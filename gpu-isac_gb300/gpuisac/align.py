@@ -4,6 +4,7 @@ on numpy arrays or torch tensors instead of EMData lists.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 
 import numpy as np
@@ -16,6 +17,30 @@ def make_config(sbj_num, ref_num, img_dim, ring_num, ring_len=256, shift_step=1.
                 shift_rng_y=1.0, aln_type=b"mref_aln") -> AlignConfig:
     return AlignConfig(sbj_num, ref_num, img_dim, ring_num, ring_len, shift_step, shift_rng_x, shift_rng_y,
                        aln_type)
+
+
+# arithmetic of the ring-summed contraction (gpuisac_set_contraction)
+CONTRACTIONS = {"fp32": 0, "bf16x3": 1}
+
+
+@contextlib.contextmanager
+def contraction(mode: str | None):
+    """Run the enclosed calls with the contraction in `mode`: "fp32" (FP32 on
+    the CUDA cores, the drop-in default) or "bf16x3" (BF16 hi/lo split on the
+    tensor cores); None leaves the current mode."""
+    if mode is None:
+        yield
+        return
+    if mode not in CONTRACTIONS:
+        raise ValueError(f"unknown contraction {mode!r} (one of {sorted(CONTRACTIONS)})")
+    L = _lib.load()
+    prev = L.gpuisac_set_contraction(CONTRACTIONS[mode])
+    if prev < 0:
+        _lib.check(L)
+    try:
+        yield
+    finally:
+        L.gpuisac_set_contraction(prev)
 
 
 def ptr_array(stack: np.ndarray):
@@ -33,13 +58,22 @@ def ptr_array(stack: np.ndarray):
 
 def multi_ref_align(particles: np.ndarray, refs: np.ndarray, ring_num: int, shift_rng_x: float,
                     shift_rng_y: float, shift_step: float = 1.0, base_shifts: np.ndarray | None = None,
-                    ring_len: int = 256, device: int = 0, mem_request: float = 0.9, d_pitch: int | None = None):
+                    ring_len: int = 256, device: int = 0, mem_request: float = 0.9, d_pitch: int | None = None,
+                    contraction_mode: str | None = None):
     """Align every particle against every reference through the C-ABI.
 
     Returns (peak_list, d): peak_list [ref][4*sbj] float32 laid out as the
     reference's caller expects (angle, sx, sy, mirror per particle), d
-    [ref][sbj] float32 peak correlations.
+    [ref][sbj] float32 peak correlations.  contraction_mode: "fp32" or
+    "bf16x3" for this call (None: the library's current mode).
     """
+    with contraction(contraction_mode):
+        return _multi_ref_align(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_step, base_shifts,
+                                ring_len, device, mem_request, d_pitch)
+
+
+def _multi_ref_align(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_step, base_shifts, ring_len,
+                     device, mem_request, d_pitch):
     L = _lib.load()
     particles = np.ascontiguousarray(particles, np.float32)
     refs = np.ascontiguousarray(refs, np.float32)
@@ -71,8 +105,17 @@ def multi_ref_align(particles: np.ndarray, refs: np.ndarray, ring_num: int, shif
 
 
 def multi_ref_align_device(particles, refs, ring_num: int, shift_rng_x: float, shift_rng_y: float,
-                           shift_step: float = 1.0, base_shifts=None, stream=None, d_out=None, peak_out=None):
-    """Device-resident form on torch CUDA tensors: returns (d [R][P], peak [R][P][4])."""
+                           shift_step: float = 1.0, base_shifts=None, stream=None, d_out=None, peak_out=None,
+                           contraction_mode: str | None = None):
+    """Device-resident form on torch CUDA tensors: returns (d [R][P], peak [R][P][4]).
+    contraction_mode: "fp32" or "bf16x3" for this call (None: the current mode)."""
+    with contraction(contraction_mode):
+        return _multi_ref_align_device(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_step,
+                                       base_shifts, stream, d_out, peak_out)
+
+
+def _multi_ref_align_device(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_step, base_shifts, stream,
+                            d_out, peak_out):
     import torch
 
     if not (particles.is_cuda and refs.is_cuda):

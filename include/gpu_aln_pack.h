@@ -149,6 +149,35 @@ const char *gpuisac_version(void);
 int gpuisac_multi_ref_align_device(const AlignConfig *cfg, const float *sbj, const float *ref,
                                    const float *base_shift, float *d_out, float *peak_out, void *stream);
 
+/* No counterpart in the reference (its contraction, cu_ccf_mult_mref at
+ * cuda/gpu_aln_noref.cu:1483-1537, is FP32 on the CUDA cores).  Arithmetic of
+ * the ring-summed contraction used by multi_ref_align and
+ * gpuisac_multi_ref_align_device:
+ *   GPUISAC_CONTRACTION_FP32    FP32 fused multiply-adds on the CUDA cores,
+ *                               the drop-in default;
+ *   GPUISAC_CONTRACTION_BF16X3  every FP32 operand split into a BF16 high part
+ *                               and the BF16 rounding of the remainder, the
+ *                               three products hi*hi + hi*lo + lo*hi
+ *                               accumulated in FP32 on the tensor cores
+ *                               (tcgen05), peak values within 1e-4 relative of
+ *                               the FP32 form.
+ * The environment variable GPUISAC_CONTRACTION=bf16x3 selects the second at
+ * load time.  gpuisac_set_contraction returns the previous mode, or -1 for an
+ * unknown one. */
+/* No counterpart in the reference (whose CUDA errors exit the process).  For
+ * failure-path tests only: while wait_iters > 0, the kernels that stage their
+ * inputs with asynchronous bulk copies (the tensor-memory CCF kernels and both
+ * kernels of the tensor-core contraction) issue no copies and give up each
+ * bounded wait after wait_iters tries of at most 20 us, so that an alignment
+ * call comes back with error code 1 ("timed out") and the context stays
+ * usable; 0 restores normal operation. */
+void gpuisac_test_stall_ccf(unsigned int wait_iters);
+
+#define GPUISAC_CONTRACTION_FP32 0
+#define GPUISAC_CONTRACTION_BF16X3 1
+int gpuisac_set_contraction(int mode);
+int gpuisac_get_contraction(void);
+
 /* No counterpart in the reference.  gpuisac_multi_ref_align_device without
  * any device memory allocation, for callers that cannot call cudaMalloc:
  * their GPU memory belongs to another allocator, or they must not pay the

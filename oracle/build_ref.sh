@@ -9,9 +9,11 @@
 # printer) and the removed field reads another int field of the same struct
 # (it is only printed by print_gpu_info).
 #
-# usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: /root/reference)
+# usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT: the argument, else $GPUISAC_REFERENCE_ROOT, else
+#   /root/reference; exits 2 when no sources are found there
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${GPUISAC_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/cuda/gpu_aln_noref.cu" ]; then

@@ -23,9 +23,25 @@ def circ_diff(a, b):
     return np.minimum(d, 360.0 - d)
 
 
-def compare(peak_g, d_g, peak_o, d_o):
-    """peak_* [R][P][4], d_* [R][P]"""
-    rel = np.abs(d_g.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), 1e-30)
+def cs_bound(ring_num, ring_len=256):
+    """Cauchy-Schwarz bound of a peak value: both polar images are normalised
+    to weighted mean 0 and weighted variance 1 (weights r+1), and the
+    unnormalised inverse FFT of the unnormalised ring spectra multiplies the
+    weighted dot product by L, so |d| <= L * L * sum_r (r+1)."""
+    return float(ring_len) * ring_len * ring_num * (ring_num + 1) / 2.0
+
+
+# Peaks below this fraction of the bound (|normalised correlation| < 1%) are
+# near-total cancellations: their rounding error is set by the magnitudes
+# summed, not by the peak, so they are held to 1e-4 of 1% of the bound.
+NEAR_ZERO = 0.01
+
+
+def compare(peak_g, d_g, peak_o, d_o, ring_num=None):
+    """peak_* [R][P][4], d_* [R][P]; with ring_num, peak values are compared
+    relative to max(|d|, NEAR_ZERO x the Cauchy-Schwarz bound)"""
+    floor = NEAR_ZERO * cs_bound(ring_num) if ring_num else 1e-30
+    rel = np.abs(d_g.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), floor)
     assert rel.max() <= PEAK_RTOL, rel.max()
     same_tuple = (peak_g[..., 1:] == peak_o[..., 1:]).all(-1) & (circ_diff(peak_g[..., 0], peak_o[..., 0]) < ANGLE_TOL)
     qg, qo = np.argmax(d_g, 0), np.argmax(d_o, 0)

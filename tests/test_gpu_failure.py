@@ -1,0 +1,48 @@
+"""Failure detection without a GPU fault: the kernels' bounded waits.
+
+Every kernel that stages its inputs with asynchronous bulk copies waits on an
+mbarrier with a bounded number of tries; on giving up it sets the device
+error word, lets its own copies and MMAs land, frees its tensor memory and
+returns, and the host call reports error code 1.  The test hook
+gpuisac_test_stall_ccf makes those kernels issue no copies -- a wait on a
+barrier that nothing completes -- with a short limit (64 tries of at most
+20 us), so the wait runs out with no copy outstanding.  The call must come
+back with the error, quickly, and the next normal call on the same context
+must give correct results.
+"""
+import os
+import time
+
+import numpy as np
+import pytest
+
+from gpuisac import GpuIsacError, synth
+
+from test_gpu_align import oracle_run, compare
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def stack():
+    return synth.make_stack(24, 64, 6, 2, 0.1, 28.0, 4711)
+
+
+@pytest.mark.parametrize("kernel,mode", [("ws", "fp32"), ("tmem", "fp32"), ("ws", "bf16x3")])
+def test_stalled_wait_returns_error_and_context_survives(gpulib, cuda, oracle_mod, stack, monkeypatch, kernel, mode):
+    from gpuisac import multi_ref_align
+    monkeypatch.setenv("GPUISAC_CCF_KERNEL", kernel)
+    gpulib.gpuisac_clear_error()
+    gpulib.gpuisac_test_stall_ccf(64)
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(GpuIsacError, match="timed out"):
+            multi_ref_align(stack.particles, stack.refs, 29, 2.0, 2.0, contraction_mode=mode)
+        assert time.perf_counter() - t0 < 30.0
+    finally:
+        gpulib.gpuisac_test_stall_ccf(0)
+        gpulib.gpuisac_clear_error()
+    # the same context, a normal call: correct results
+    pl, d = multi_ref_align(stack.particles, stack.refs, 29, 2.0, 2.0, contraction_mode=mode)
+    peak_o, d_o = oracle_run(oracle_mod, stack.particles, stack.refs, 29, 2.0, tex=gpulib.get_texture_limit(64))
+    compare(pl.reshape(6, 24, 4), d, peak_o, d_o)

@@ -22,7 +22,11 @@ def circ_diff(a, b):
     return np.minimum(d, 360.0 - d)
 
 
-def run(gpulib, fn, cfg, parts, refs, base, cuda):
+def run(gpulib, fn, cfg, parts, refs, base, cuda, free_delta=None):
+    """One call of entry point fn into fresh NaN-filled outputs.  With
+    free_delta (a list), the device's free memory right before and right
+    after the call (outputs already allocated, the stream idle on both
+    sides) is measured and the change appended."""
     import torch
 
     from gpuisac import _lib
@@ -30,11 +34,15 @@ def run(gpulib, fn, cfg, parts, refs, base, cuda):
     d = torch.full((R, P), float("nan"), dtype=torch.float32, device=cuda)
     pk = torch.full((R, P, 4), float("nan"), dtype=torch.float32, device=cuda)
     st = torch.cuda.current_stream(cuda)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(cuda)[0]
     rc = getattr(gpulib, fn)(ctypes.byref(cfg), parts.data_ptr(), refs.data_ptr(), base.data_ptr(), d.data_ptr(),
                              pk.data_ptr(), st.cuda_stream)
     if rc:
         _lib.check(gpulib)
     torch.cuda.synchronize()
+    if free_delta is not None:
+        free_delta.append(free0 - torch.cuda.mem_get_info(cuda)[0])
     return d.cpu().numpy(), pk.cpu().numpy()
 
 
@@ -50,13 +58,17 @@ def test_noalloc_matches_allocating_entry_point(gpulib, cuda):
     base = torch.from_numpy(np.random.default_rng(5).uniform(-1.5, 1.5, (300, 2)).astype(np.float32)).to(cuda)
     cfg = make_config(300, 20, 76, 35, 256, 1.0, 3.0, 3.0)
     d_ref, pk_ref = run(gpulib, "gpuisac_multi_ref_align_device", cfg, parts, refs, base, cuda)
+    deltas = []
     for _ in range(2):  # two calls in a row share the array
-        d, pk = run(gpulib, "gpuisac_multi_ref_align_device_noalloc", cfg, parts, refs, base, cuda)
+        d, pk = run(gpulib, "gpuisac_multi_ref_align_device_noalloc", cfg, parts, refs, base, cuda, deltas)
         assert np.isfinite(d).all() and np.isfinite(pk).all()
         rel = np.abs(d.astype(np.float64) - d_ref) / np.maximum(np.abs(d_ref), 1e-30)
         assert rel.max() <= PEAK_RTOL
         assert (pk[..., 1:] == pk_ref[..., 1:]).all()
         assert circ_diff(pk[..., 0], pk_ref[..., 0]).max() < ANGLE_TOL
+    # the first call on a device may load the library's device code and its
+    # static array (module loading is lazy); the second allocates nothing
+    assert deltas[1] == 0, f"device free memory changed by {deltas[1]} bytes across a call"
 
 
 def test_noalloc_rejects_workloads_beyond_its_array(gpulib, cuda):
