@@ -649,6 +649,100 @@ def precision_vs_fp64(dev, n=64, R=200):
             "oracle_seconds": t}
 
 
+def spectra_roofline(w, P, steps, spec_ms, spec_launches, hbm_peak, peak_kind, out_bytes_per_row):
+    """resample + FFT stage: images read once per shift row, spectra (or
+    operands) written"""
+    S = w["n_shifts"]
+    spec_avg_ms = spec_ms / max(spec_launches, 1)
+    spec_bytes = (P * w["img_dim"] ** 2 * 4 * S + P * S * out_bytes_per_row) * steps / max(spec_launches, 1)
+    return {"avg_launch_ms": spec_avg_ms, "bytes_per_launch": spec_bytes,
+            "achieved_gbs": spec_bytes / (spec_avg_ms / 1000.0) / 1e9 if spec_avg_ms else None,
+            "hbm_peak_gbs": hbm_peak, "hbm_peak_kind": peak_kind}
+
+
+def fp32_roofline(dev, w, P, R, steps, ccf_ms, ccf_launches, spec_ms, spec_launches, hbm_peak, bf16_peak, peak_kind):
+    """The fused FP32 CCF / inverse-FFT / peak kernel: algorithmic contraction
+    FLOPs per launch over its average launch time, against the FP32 rate of
+    the CUDA cores (the plain path's ceiling), measured here with cuBLAS SGEMM
+    as the bf16 peak is measured with a bf16 GEMM; the nominal FMA rate (152
+    SMs x 128 lanes x 2 flops x max SM clock) and the bf16 tensor peak beside
+    it.  Traffic: the 3,000-particle ncu capture's DRAM bytes per alignment
+    (profiles/ccf_peak_traffic.txt) scaled to a launch."""
+    S = w["n_shifts"]
+    alignments = P * R
+    flops_per_alignment = 8.0 * S * (w["ring_len"] // 2 + 1) * w["rings"]
+    flops_per_launch = flops_per_alignment * alignments * steps / max(ccf_launches, 1)
+    ccf_avg_ms = ccf_ms / max(ccf_launches, 1)
+    achieved_tflops = flops_per_launch / (ccf_avg_ms / 1000.0) / 1e12
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "ccf_peak_traffic.txt")
+    if os.path.exists(tfile):
+        for ln in open(tfile):
+            if ln.startswith("dram_bytes_per_particle_ref:"):
+                traffic = float(ln.split(":")[1]) * alignments * steps / max(ccf_launches, 1)
+    fp32_nominal = fp32_nominal_tflops()
+    fp32_peak = fp32_measured_tflops(dev)
+    return {"bound": "fp32-fma", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved_tflops / fp32_peak, "traffic": traffic, "kernel": "ccf_peak",
+            "peak_kind": "measured: cuBLAS SGEMM (TF32 off, CUDA cores) on this GPU, 8192^3",
+            "fp32_nominal_peak": fp32_nominal, "frac_of_fp32_nominal": achieved_tflops / fp32_nominal,
+            "flops_per_launch": flops_per_launch, "avg_launch_ms": ccf_avg_ms,
+            "kernel_share": ccf_ms / max(ccf_ms + spec_ms, 1e-9),
+            "frac_of_bf16_tensor_peak": achieved_tflops / bf16_peak, "bf16_peak": bf16_peak,
+            "bf16_peak_kind": peak_kind,
+            "spectra": spectra_roofline(w, P, steps, spec_ms, spec_launches, hbm_peak, peak_kind,
+                                        w["rings"] * 128 * 8)}
+
+
+def split_roofline(L, w, P, R, steps, split_ms, spec_ms, spec_launches, hbm_peak, bf16_peak, peak_kind):
+    """The tensor-core contraction's two kernels.  Both move the pair spectra
+    Z (2 KB per (particle x shift, reference) pair) through HBM, so both are
+    HBM-bound: algorithmic bytes per launch = Z written (ccf_mma_kernel, plus
+    the subject operands it reads) or Z read (zfft_peak_kernel, plus d and
+    peak_list written), over the average launch time, against the measured
+    copy bandwidth.  The MMA kernel's tensor-pipe work is reported beside it:
+    3 BF16 products x 2 x 128 x N x 16 FLOPs per tcgen05.mma, and the
+    algorithmic contraction FLOPs 8 S (L/2+1) N_r per alignment."""
+    from gpuisac.align import split_plan
+    S, NR = w["n_shifts"], w["rings"]
+    pl = split_plan(NR, S, R)
+    alignments = P * R
+    z_bytes = float(P) * R * S * 2048
+    sop_bytes = float(P) * pl["n_blocks"] * 128 * 2 * pl["kg"] * pl["rga"] * 128
+    out_bytes = float(P) * R * 20
+    ks = (pl["kg"] + (pl["kg"] & 1)) // 2
+    mma_flops = float(P) * pl["n_blocks"] * pl["n_rtiles"] * 128 * ks * 3 * 2 * 128 * pl["n_cols"] * 16
+    alg_flops = 8.0 * S * (w["ring_len"] // 2 + 1) * NR * alignments
+    kern = {}
+    for name, byts in (("ccf_mma", z_bytes + sop_bytes), ("zfft_peak", z_bytes + out_bytes)):
+        k = split_ms[name]
+        launches = max(k["launches"] // max(steps, 1), 1)
+        avg_ms = k["ms_per_step"] / launches
+        per_launch = byts / launches
+        kern[name] = {"avg_launch_ms": avg_ms, "launches_per_step": launches, "bytes_per_launch": per_launch,
+                      "achieved_gbs": per_launch / (avg_ms / 1000.0) / 1e9, "ms_per_step": k["ms_per_step"]}
+    mma_s = split_ms["ccf_mma"]["ms_per_step"] / 1000.0
+    kern["ccf_mma"]["tensor"] = {
+        "mma_flops_per_step": mma_flops, "achieved_tflops": mma_flops / mma_s / 1e12,
+        "frac_of_bf16_peak": mma_flops / mma_s / 1e12 / bf16_peak, "bf16_peak": bf16_peak,
+        "algorithmic_flops_per_step": alg_flops, "algorithmic_tflops": alg_flops / mma_s / 1e12}
+    dom = max(kern, key=lambda n: kern[n]["ms_per_step"])
+    d = kern[dom]
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", f"{dom}_traffic.txt")
+    if os.path.exists(tfile):
+        for ln in open(tfile):
+            if ln.startswith("dram_bytes_per_pair:"):
+                traffic = float(ln.split(":")[1]) * alignments * S / d["launches_per_step"]
+    total_ms = sum(k["ms_per_step"] for k in kern.values()) + spec_ms / max(steps, 1)
+    return {"bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm_peak, "unit": "GB/s",
+            "frac": d["achieved_gbs"] / hbm_peak, "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
+            "avg_launch_ms": d["avg_launch_ms"], "kernel_share": d["ms_per_step"] / max(total_ms, 1e-9),
+            "plan": pl, "kernels": kern,
+            "spectra": spectra_roofline(w, P, steps, spec_ms, spec_launches, hbm_peak, peak_kind,
+                                        2 * 2 * 2 * pl["kg"] * 8 * 128)}
+
+
 def bench_ours(args):
     import torch
 
@@ -677,6 +771,8 @@ def bench_ours(args):
     peak_out = torch.empty((R, P, 4), dtype=torch.float32, device=dev)
     cfg = make_config(P, R, w["img_dim"], w["rings"], 256, 1.0, sr, sr)
     stream = torch.cuda.Stream(dev)
+    from gpuisac.align import CONTRACTIONS
+    L.gpuisac_set_contraction(CONTRACTIONS[args.contraction])
 
     def step():
         rc = L.gpuisac_multi_ref_align_device(ctypes.byref(cfg), parts_d.data_ptr(), refs_d.data_ptr(),
@@ -724,6 +820,10 @@ def bench_ours(args):
     ccf_launches, ccf_ms = n_l.value, t_l.value
     L.gpuisac_kernel_time(b"polar_spectra", ctypes.byref(n_l), ctypes.byref(t_l))
     spec_launches, spec_ms = n_l.value, t_l.value
+    split_ms = {}
+    for kname in ("ccf_mma", "zfft_peak"):
+        L.gpuisac_kernel_time(kname.encode(), ctypes.byref(n_l), ctypes.byref(t_l))
+        split_ms[kname] = {"launches": n_l.value, "ms_per_step": t_l.value / args.steps}
     L.gpuisac_profile(0)
     if world > 1:
         from gpuisac import replicas
@@ -736,36 +836,13 @@ def bench_ours(args):
     hbm_peak, bf16_peak, peak_kind = peaks()
     S = w["n_shifts"]
     flops_per_alignment = 8.0 * S * (w["ring_len"] // 2 + 1) * w["rings"]
-    flops_per_launch = flops_per_alignment * alignments * args.steps / max(ccf_launches, 1)
-    ccf_avg_ms = ccf_ms / max(ccf_launches, 1)
-    achieved_tflops = flops_per_launch / (ccf_avg_ms / 1000.0) / 1e12
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "ccf_peak_traffic.txt")
-    if os.path.exists(tfile):
-        for ln in open(tfile):
-            if ln.startswith("dram_bytes_per_particle_ref:"):
-                traffic = float(ln.split(":")[1]) * alignments * args.steps / max(ccf_launches, 1)
-    # the plain path's contraction runs in FP32 on CUDA cores, so its ceiling
-    # is the FP32 rate of the CUDA cores: measured here with cuBLAS SGEMM (as
-    # the bf16 peak is measured with a bf16 GEMM), the nominal FMA rate (152
-    # SMs x 128 lanes x 2 flops x max SM clock) beside it; the bf16 tensor
-    # peak is reported too
-    fp32_nominal = fp32_nominal_tflops()
-    fp32_peak = fp32_measured_tflops(dev)
-    spec_avg_ms = spec_ms / max(spec_launches, 1)
-    # resample + FFT stage: images read once per shift row, spectra written
-    spec_bytes = (P * w["img_dim"] ** 2 * 4 * S + P * S * w["rings"] * 128 * 8) * args.steps / max(spec_launches, 1)
-    roofline = {"bound": "fp32-fma", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": achieved_tflops / fp32_peak, "traffic": traffic, "kernel": "ccf_peak",
-                "peak_kind": "measured: cuBLAS SGEMM (TF32 off, CUDA cores) on this GPU, 8192^3",
-                "fp32_nominal_peak": fp32_nominal, "frac_of_fp32_nominal": achieved_tflops / fp32_nominal,
-                "flops_per_launch": flops_per_launch, "avg_launch_ms": ccf_avg_ms,
-                "kernel_share": ccf_ms / max(ccf_ms + spec_ms, 1e-9),
-                "frac_of_bf16_tensor_peak": achieved_tflops / bf16_peak, "bf16_peak": bf16_peak,
-                "bf16_peak_kind": peak_kind,
-                "spectra": {"avg_launch_ms": spec_avg_ms, "bytes_per_launch": spec_bytes,
-                            "achieved_gbs": spec_bytes / (spec_avg_ms / 1000.0) / 1e9 if spec_avg_ms else None,
-                            "hbm_peak_gbs": hbm_peak, "hbm_peak_kind": peak_kind}}
+    if args.contraction == "bf16x3":
+        roofline = split_roofline(L, w, P, R, args.steps, split_ms, spec_ms, spec_launches, hbm_peak, bf16_peak,
+                                  peak_kind)
+    else:
+        roofline = fp32_roofline(dev, w, P, R, args.steps, ccf_ms, ccf_launches, spec_ms, spec_launches, hbm_peak,
+                                 bf16_peak, peak_kind)
+
 
     # ---- end to end through the reference-facing C-ABI ----
     e2e = None
@@ -836,9 +913,12 @@ def bench_ours(args):
         line = {"metric": metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded phantoms, {P} particles/GPU)",
-                "config": dict(WORKLOAD, particles=P, path="plain FP32 CUDA-core contraction", autotune=tune,
+                "config": dict(WORKLOAD, particles=P, autotune=tune,
+                               path="plain FP32 CUDA-core contraction" if args.contraction == "fp32" else
+                               "BF16 hi/lo split contraction on the tensor cores (tcgen05), pair spectra through HBM",
                                l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                "split_kernels": split_ms if args.contraction == "bf16x3" else None,
                 "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk,
                 "assign_groups": assign_blk, "multigroup": multigroup_blk, "prealign": prealign_blk}
         print(json.dumps(line), flush=True)
@@ -868,6 +948,9 @@ def main():
     ap.add_argument("--no-multigroup", action="store_true", help="skip the multigroup (stability test) block")
     ap.add_argument("--no-prealign", action="store_true", help="skip the pre-alignment block")
     ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")
+    ap.add_argument("--contraction", choices=["fp32", "bf16x3"], default="fp32",
+                    help="ring-summed contraction of the timed search: fp32 (CUDA cores) or bf16x3 "
+                         "(BF16 hi/lo split on the tensor cores)")
     ap.add_argument("--learned-particles", type=int, default=LEARNED["particles"])
     ap.add_argument("--learned-train", type=int, default=LEARNED["train_alignments"])
     ap.add_argument("--learned-train-largebox", type=int, default=None)

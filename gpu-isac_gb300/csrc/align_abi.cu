@@ -998,6 +998,22 @@ int gpuisac_set_contraction(int mode)
 
 int gpuisac_get_contraction(void) { return contraction_mode(); }
 
+int gpuisac_split_plan(unsigned int ring_num, unsigned int n_shift, unsigned int n_ref, unsigned int* fields,
+                       unsigned int n_fields)
+{
+    SplitPlan p;
+    if (!split_plan(ring_num, n_shift, n_ref, p)) {
+        set_error(E_UNSUPPORTED, "no tensor-core tile plan for %u rings, %u shifts, %u references", ring_num, n_shift,
+                  n_ref);
+        return E_UNSUPPORTED;
+    }
+    const unsigned v[10] = {p.n_blocks, p.block, p.zw, p.kg, p.rga, p.rblock, p.n_rtiles, p.n_cols, p.n_stages,
+                            p.fft_groups};
+    for (unsigned i = 0; fields && i < n_fields && i < 10; i++)
+        fields[i] = v[i];
+    return 0;
+}
+
 void gpuisac_profile(int on)
 {
     std::lock_guard<std::mutex> lk(g_api_mu);

@@ -94,7 +94,9 @@ __host__ __device__ constexpr uint32_t mma_idesc(uint32_t n)
     return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 
-constexpr int kMmaThreads = 192;     // warp 0 copies, warp 1 MMA, warps 2-5 drain
+constexpr int kDrainWarps = 16;      // four per tensor-memory lane quadrant
+constexpr int kDrainPerQuad = kDrainWarps / 4;
+constexpr int kMmaThreads = 64 + 32 * kDrainWarps; // warp 0 copies, warp 1 MMA, warps 2.. drain
 constexpr uint32_t kMmaTailPad = 2048; // 16 row groups x 128 bytes
 constexpr uint32_t kAccStride = 256; // tensor-memory columns between the two accumulators
 constexpr uint32_t kMmaTmemCols = 512;
@@ -147,7 +149,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
         }
         for (int i = 0; i < 2; i++) {
             mbar_init(accf + i, 1);
-            mbar_init(acce + i, 128);
+            mbar_init(acce + i, 32 * kDrainWarps);
         }
         mbar_init(done, 1);
         *abort_flag = 0;
@@ -242,9 +244,14 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
         }
     } else {
         // ================= drain: accumulators -> Z =================
-        const int quad = warp & 3;              // tensor-memory lanes 32 quad .. 32 quad + 31
-        const unsigned row = 32 * quad + lane;  // operand row = 2 shift + {0: a, 1: b}
-        const unsigned sl = row >> 1;           // shift within the block
+        // kDrainPerQuad warps per lane quadrant share a slot's columns: chunks
+        // of 16 columns (8 references) go round-robin between them, the next
+        // chunk's tensor-memory load in flight while the current one is
+        // written out
+        const int quad = warp & 3;                  // tensor-memory lanes 32 quad .. 32 quad + 31
+        const unsigned part = (unsigned)(warp - 2) >> 2; // which chunks: part, part + kDrainPerQuad, ...
+        const unsigned row = 32 * quad + lane;      // operand row = 2 shift + {0: a, 1: b}
+        const unsigned sl = row >> 1;               // shift within the block
         const bool is_b = row & 1u;
         uint32_t it = 0;
         for (unsigned item = blockIdx.x; item < w.n_items && !failed; item += gridDim.x) {
@@ -257,6 +264,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
             float2* zbase = w.z + ((size_t)(p * w.n_ref + q0) * w.n_blocks + b) * kRingLen * w.zw + sl;
             const size_t zq = (size_t)w.n_blocks * kRingLen * w.zw; // between references
             const unsigned nchunk = (2 * nq + 15) / 16;
+            const unsigned nj = nchunk > part ? (nchunk - part + kDrainPerQuad - 1) / kDrainPerQuad : 0;
             for (unsigned k = 0; k < (unsigned)kSlots; k++, it++) {
                 const uint32_t buf = it & 1u;
                 const bool ok = mbar_wait_abort(accf + buf, (it >> 1) & 1u, abort_flag, wlim);
@@ -268,10 +276,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
                 const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + buf * kAccStride;
                 // Z[k] (a rows) and Z[256 - k] (b rows); slot 0: Z[0], Z[128]
                 const size_t zoff = (size_t)(is_b ? (k ? kRingLen - k : kSlots) : k) * w.zw;
-                for (unsigned c = 0; c < nchunk; c++) {
-                    float r[16];
-                    tmem_ld16_async(taddr + 16 * c, r);
-                    tmem_wait_ld16(r);
+                auto write_chunk = [&](const float (&r)[16], unsigned c) {
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const float u = r[2 * j], v = r[2 * j + 1];
@@ -290,8 +295,29 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
                             } else {
                                 zv = is_b ? make_float2(a3, a4) : make_float2(a1, a2);
                             }
-                            zbase[ql * zq + zoff] = zv;
+                            __stcs(zbase + ql * zq + zoff, zv); // streamed: read back only by the next kernel
                         }
+                    }
+                };
+                if (nj) {
+                    float ra[16], rb[16];
+                    tmem_ld16_async(taddr + 16 * part, ra);
+                    tmem_wait_ld16(ra);
+                    for (unsigned j = 0; j < nj; j += 2) {
+                        const unsigned ca = part + kDrainPerQuad * j, cb = ca + kDrainPerQuad;
+                        const bool more_b = j + 1 < nj;
+                        if (more_b)
+                            tmem_ld16_async(taddr + 16 * cb, rb);
+                        write_chunk(ra, ca);
+                        if (!more_b)
+                            break;
+                        tmem_wait_ld16(rb);
+                        const bool more_a = j + 2 < nj;
+                        if (more_a)
+                            tmem_ld16_async(taddr + 16 * (cb + kDrainPerQuad), ra);
+                        write_chunk(rb, cb);
+                        if (more_a)
+                            tmem_wait_ld16(ra);
                     }
                 }
                 tmem_fence_before();
@@ -313,9 +339,10 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
 
 // ============================================================================
 // inverse FFT + peak search of the pair spectra Z, one (particle, reference)
-// per work item; RR shifts per 16-thread group and shift block
+// per work item, one 16-thread group per shift of a block (up to
+// kSplitMaxBlock = 49 groups, 784 threads)
 template <int RR>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(16 * kSplitMaxBlock, 1)
 zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -325,8 +352,8 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
     float2* const zb0 = reinterpret_cast<float2*>(smem_raw);
     float2* const zb1 = reinterpret_cast<float2*>(smem_raw + zbuf_bytes);
     float2* tw = reinterpret_cast<float2*>(smem_raw + 2 * zbuf_bytes); // [16][kTwRow]
-    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);    // [groups]
-    uint64_t* full = reinterpret_cast<uint64_t*>(slots + 32);          // [2]
+    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);    // [2][64] parked bests of two items
+    uint64_t* full = reinterpret_cast<uint64_t*>(slots + 128);         // [2]
     volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 2);
 
     const int tid = threadIdx.x;
@@ -369,31 +396,81 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
 
     const int g = tid >> 4, l = tid & 15;
     const unsigned gmask = 0xffffu << (tid & 16);
+    // merge of a finished item by warp 0: the groups' parked bests reduced
+    // with the reference's order (better(); equal entries: the lower group,
+    // which holds the lower shifts), then the parabola and the outputs
+    auto merge = [&](unsigned item, const PeakSlot* sl) {
+        const int lane = tid & 31;
+        unsigned bi = (unsigned)lane < groups ? (unsigned)lane : 0u;
+        float v = sl[bi].v;
+        unsigned h = sl[bi].h, t = sl[bi].t;
+        if ((unsigned)lane + 32 < groups) { // up to 64 groups: two per lane
+            const PeakSlot& o = sl[lane + 32];
+            if (better(o.v, o.h, o.t, v, h, t)) {
+                v = o.v;
+                h = o.h;
+                t = o.t;
+                bi = lane + 32;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float v2 = __shfl_xor_sync(0xffffffffu, v, off);
+            const unsigned h2 = __shfl_xor_sync(0xffffffffu, h, off), t2 = __shfl_xor_sync(0xffffffffu, t, off);
+            const unsigned b2 = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (better(v2, h2, t2, v, h, t) || (v2 == v && h2 == h && t2 == t && b2 < bi)) {
+                v = v2;
+                h = h2;
+                t = t2;
+                bi = b2;
+            }
+        }
+        if (lane == 0) {
+            const PeakSlot& ps = sl[bi];
+            const bool mirror = ps.h >= w.n_shift;
+            const unsigned sidx = mirror ? ps.h - w.n_shift : ps.h;
+            const float angle =
+                w.rule == kPeakPreAlign ? pre_peak_angle(ps.nb, ps.t, mirror) : peak_angle(ps.nb, ps.t, mirror);
+            const unsigned p = item / w.n_ref, q = item - p * w.n_ref;
+            const unsigned pg = w.p_first + p;
+            const float bx = w.base ? w.base[pg].x : 0.f, by = w.base ? w.base[pg].y : 0.f;
+            const float2 sf = w.shifts_f[sidx];
+            const size_t o = (size_t)q * w.p_total + pg;
+            w.d_out[o] = ps.v;
+            w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+        }
+    };
     PeakState st;
     st.reset(w.rule);
     bool failed = false;
-    unsigned u = 0;
+    unsigned u = 0, n_done = 0;           // items finished (their bests parked)
+    bool pending = false;                 // an item parked and not merged yet
+    unsigned pending_item = 0;
     for (; u < n_units; u++) {
         const unsigned buf = u & 1u, item = unit_item(u), b = u % w.n_blocks;
         const unsigned s0 = b * w.block, nsb = min(w.block, w.n_shift - s0);
         const bool ok = mbar_wait(full + buf, (u >> 1) & 1u, wlim);
-        if (!__syncthreads_and(ok)) {
-            failed = true;
-            break;
-        }
         float2* const zcur = buf ? zb1 : zb0;
         // this group's shift columns into registers
         float2 x[RR][16];
 #pragma unroll
         for (int rr = 0; rr < RR; rr++) {
             const unsigned sl = g + rr * groups;
-            if (sl < nsb) {
+            if (ok && sl < nsb) {
 #pragma unroll
                 for (int m = 0; m < 16; m++)
                     x[rr][m] = zcur[(l + 16 * m) * w.zw + sl];
             }
         }
-        __syncthreads(); // the buffer now serves as the groups' FFT workspaces
+        // every column is in registers: the buffer now serves as the groups'
+        // FFT workspaces; the parks of the last finished item are visible
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        if (pending && tid < 32)
+            merge(pending_item, slots + 64 * ((n_done - 1) & 1u));
+        pending = false;
         float2* gz = zcur + g * kPairStride;
 #pragma unroll
         for (int rr = 0; rr < RR; rr++) {
@@ -402,33 +479,19 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
                 fft_peak_regs<true>(x[rr], gz, tw + l * kTwRow, l, gmask, s0 + sl, w.n_shift, st, w.rule);
         }
         if (b == w.n_blocks - 1) {
-            // every shift of the pair has been searched: merge the groups
-            park_slot(slots, st, g, l);
-            __syncthreads();
-            if (tid == 0) {
-                unsigned best = 0;
-                for (unsigned i = 1; i < groups; i++)
-                    if (better(slots[i].v, slots[i].h, slots[i].t, slots[best].v, slots[best].h, slots[best].t))
-                        best = i;
-                const PeakSlot& ps = slots[best];
-                const bool mirror = ps.h >= w.n_shift;
-                const unsigned sidx = mirror ? ps.h - w.n_shift : ps.h;
-                const float angle =
-                    w.rule == kPeakPreAlign ? pre_peak_angle(ps.nb, ps.t, mirror) : peak_angle(ps.nb, ps.t, mirror);
-                const unsigned p = item / w.n_ref, q = item - p * w.n_ref;
-                const unsigned pg = w.p_first + p;
-                const float bx = w.base ? w.base[pg].x : 0.f, by = w.base ? w.base[pg].y : 0.f;
-                const float2 sf = w.shifts_f[sidx];
-                const size_t o = (size_t)q * w.p_total + pg;
-                w.d_out[o] = ps.v;
-                w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
-            }
+            // every shift of the pair has been searched: park the group's best
+            park_slot(slots + 64 * (n_done & 1u), st, g, l);
             st.reset(w.rule);
+            pending = true;
+            pending_item = item;
+            n_done++;
         }
-        __syncthreads(); // buffer and slots free
+        __syncthreads(); // the buffer is free; the parks are visible
         if (tid == 0 && u + 2 < n_units)
             issue(u + 2);
     }
+    if (!failed && pending && tid < 32)
+        merge(pending_item, slots + 64 * ((n_done - 1) & 1u));
     if (failed && tid == 0) {
         atomicExch(err, 1u);
         // copies in flight land before the CTA ends (bounded)
@@ -459,7 +522,7 @@ static size_t mma_smem(const SplitPlan& p) { return (size_t)p.n_stages * mma_sta
 static size_t fft_smem(const SplitPlan& p)
 {
     const size_t zbuf = std::max((size_t)kRingLen * p.zw * sizeof(float2), (size_t)p.fft_groups * kPairStride * sizeof(float2));
-    return 2 * zbuf + 16 * kTwRow * sizeof(float2) + 32 * sizeof(PeakSlot) + 64;
+    return 2 * zbuf + 16 * kTwRow * sizeof(float2) + 128 * sizeof(PeakSlot) + 64;
 }
 
 bool split_plan(unsigned ring_num, unsigned n_shift, unsigned n_ref, SplitPlan& p)
@@ -471,8 +534,8 @@ bool split_plan(unsigned ring_num, unsigned n_shift, unsigned n_ref, SplitPlan& 
     p.zw = p.block | 1u; // odd row length: the FFT's column reads hit distinct banks
     p.kg = (ring_num + 7) / 8;
     p.rga = (2 * p.block + 7) / 8;
-    p.rounds = p.block > 32 ? 2 : 1;
-    p.fft_groups = (p.block + p.rounds - 1) / p.rounds;
+    p.rounds = 1;
+    p.fft_groups = p.block;
     const size_t cap = std::min<size_t>((size_t)smem_optin_max(), 227 * 1024);
     // references per tile: as many as N = 2 x refs <= 256 allows with at
     // least two operand stages, tiles balanced
@@ -587,15 +650,9 @@ cudaError_t launch_zfft_peak(const SplitPlan& p, const float2* z, unsigned n_par
     const size_t fs = fft_smem(p);
     const unsigned grid = std::min<unsigned>(n_part * n_ref, device_sms());
     cudaError_t e;
-    if (p.rounds == 1) {
-        if ((e = opt_in_smem_k(zfft_peak_kernel<1>, fs)) != cudaSuccess)
-            return e;
-        zfft_peak_kernel<1><<<grid, 16 * p.fft_groups, fs, stream>>>(fw, twiddle, err);
-    } else {
-        if ((e = opt_in_smem_k(zfft_peak_kernel<2>, fs)) != cudaSuccess)
-            return e;
-        zfft_peak_kernel<2><<<grid, 16 * p.fft_groups, fs, stream>>>(fw, twiddle, err);
-    }
+    if ((e = opt_in_smem_k(zfft_peak_kernel<1>, fs)) != cudaSuccess)
+        return e;
+    zfft_peak_kernel<1><<<grid, 16 * p.fft_groups, fs, stream>>>(fw, twiddle, err);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

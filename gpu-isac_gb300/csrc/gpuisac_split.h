@@ -26,7 +26,7 @@ struct SplitPlan {
     unsigned n_cols = 0;     // MMA N: 2 x rblock rounded up to 16
     unsigned rgb = 0;        // row groups of a reference tile (n_cols / 8)
     unsigned n_stages = 0;   // operand stages of the MMA kernel
-    unsigned rounds = 1;     // shifts per FFT group and block
+    unsigned rounds = 1;     // shifts per FFT group and block (1: a group per shift)
     unsigned fft_groups = 0; // 16-thread FFT groups of the FFT kernel
     size_t sop_slot = 0;     // bytes of one subject tile's slot (hi + lo)
     size_t rop_slot = 0;     // bytes of one reference tile's slot (hi + lo)

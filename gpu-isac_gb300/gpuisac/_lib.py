@@ -49,6 +49,7 @@ EXPORTS = (
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
     "gpuisac_ref_free_averages", "gpuisac_set_contraction", "gpuisac_get_contraction", "gpuisac_test_stall_ccf",
+    "gpuisac_split_plan",
 )
 
 
@@ -186,6 +187,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_get_contraction.restype = ctypes.c_int
     L.gpuisac_test_stall_ccf.argtypes = [ctypes.c_uint]
     L.gpuisac_test_stall_ccf.restype = None
+    L.gpuisac_split_plan.argtypes = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint),
+                                     ctypes.c_uint]
+    L.gpuisac_split_plan.restype = ctypes.c_int
     if path is None:
         _lib = L
     return L

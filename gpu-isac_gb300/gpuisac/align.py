@@ -43,6 +43,19 @@ def contraction(mode: str | None):
         L.gpuisac_set_contraction(prev)
 
 
+SPLIT_PLAN_FIELDS = ("n_blocks", "block", "zw", "kg", "rga", "rblock", "n_rtiles", "n_cols", "n_stages",
+                     "fft_groups")
+
+
+def split_plan(ring_num: int, n_shift: int, n_ref: int) -> dict:
+    """The tensor-core contraction's tile plan for a shape (gpuisac_split_plan)."""
+    L = _lib.load()
+    f = (ctypes.c_uint * len(SPLIT_PLAN_FIELDS))()
+    if L.gpuisac_split_plan(ring_num, n_shift, n_ref, f, len(SPLIT_PLAN_FIELDS)):
+        _lib.check(L)
+    return dict(zip(SPLIT_PLAN_FIELDS, list(f)))
+
+
 def ptr_array(stack: np.ndarray):
     """float** over the images of a C-contiguous float32 [n][D][D] stack (the
     reference's get_c_ptr_array, bin/sp_isac2_gpu.py:166-174)."""

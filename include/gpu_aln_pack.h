@@ -177,6 +177,13 @@ void gpuisac_test_stall_ccf(unsigned int wait_iters);
 #define GPUISAC_CONTRACTION_BF16X3 1
 int gpuisac_set_contraction(int mode);
 int gpuisac_get_contraction(void);
+/* No counterpart in the reference.  The tensor-core contraction's tile plan
+ * for a shape, for measurement: fields[0..9] = shift blocks, shifts per
+ * block, Z row length, K groups of 8 rings, subject row groups, references
+ * per tile, reference tiles, MMA N, operand stages, FFT groups (as many as
+ * n_fields holds).  Returns 0, or 4 when the shape has no plan. */
+int gpuisac_split_plan(unsigned int ring_num, unsigned int n_shift, unsigned int n_ref, unsigned int *fields,
+                       unsigned int n_fields);
 
 /* No counterpart in the reference.  gpuisac_multi_ref_align_device without
  * any device memory allocation, for callers that cannot call cudaMalloc:
