@@ -125,20 +125,28 @@ __device__ __forceinline__ void fft_peak_regs(float2 (&x)[16], float2* gz, const
             st.nb = wf[((unsigned)l - 3u) & (kRingLen - 1)];
         __syncwarp(gmask);
     }
+    // group maximum of each mirror first (the two reductions side by side);
+    // the first index is only needed when a candidate can replace the
+    // running best
+    float vm[2] = {x[perm16(0)].x, x[perm16(0)].y};
+#pragma unroll
+    for (int k2 = 1; k2 < 16; k2++) {
+        vm[0] = fmaxf(vm[0], x[perm16(k2)].x);
+        vm[1] = fmaxf(vm[1], x[perm16(k2)].y);
+    }
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) {
+        const float o0 = __shfl_xor_sync(gmask, vm[0], off), o1 = __shfl_xor_sync(gmask, vm[1], off);
+        vm[0] = fmaxf(vm[0], o0);
+        vm[1] = fmaxf(vm[1], o1);
+    }
+    // lane 0's values for the whole group keep every branch below
+    // group-uniform, NaN inputs included
+    vm[0] = __shfl_sync(gmask, vm[0], 0, 16);
+    vm[1] = __shfl_sync(gmask, vm[1], 0, 16);
 #pragma unroll
     for (int mir = 0; mir < 2; mir++) {
-        // group maximum first; the first index is only needed when this
-        // candidate can replace the running best
-        float v = mir ? x[perm16(0)].y : x[perm16(0)].x;
-#pragma unroll
-        for (int k2 = 1; k2 < 16; k2++)
-            v = fmaxf(v, mir ? x[perm16(k2)].y : x[perm16(k2)].x);
-#pragma unroll
-        for (int off = 8; off > 0; off >>= 1)
-            v = fmaxf(v, __shfl_xor_sync(gmask, v, off));
-        // lane 0's value for the whole group keeps every branch below
-        // group-uniform, NaN inputs included
-        v = __shfl_sync(gmask, v, 0, 16);
+        const float v = vm[mir];
         if (!(v >= st.bv))
             continue;
         unsigned t = 0xffffffffu;

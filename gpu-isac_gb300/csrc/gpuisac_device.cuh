@@ -26,14 +26,28 @@ __device__ __forceinline__ float2 cmul_i(float2 a)
     return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// 4-point DFT in place, X[k] = sum_n x[n] w4^(SIGN n k), w4 = e^(2 pi i / 4)
-template <int SIGN>
+// 4-point DFT in place, X[k] = sum_n x[n] w4^(SIGN n k), w4 = e^(2 pi i / 4).
+// The component-wise sums and differences run as packed two-lane FP32
+// instructions (x - y as fma(y, -1, x): the product is exact, so each lane
+// rounds exactly as a scalar subtraction); the two outputs that need the
+// multiplication by +-i swap components and stay scalar.
+template <int SIGN, bool kPacked = true>
 __device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3)
 {
-    float2 a = cadd(x0, x2), b = csub(x0, x2);
-    float2 c = cadd(x1, x3), d = cmul_i<SIGN>(csub(x1, x3));
-    x0 = cadd(a, c);
-    x2 = csub(a, c);
+    if (!kPacked) { // the same sums in scalar instructions (fewer live registers)
+        const float2 a = cadd(x0, x2), b = csub(x0, x2);
+        const float2 c = cadd(x1, x3), d = cmul_i<SIGN>(csub(x1, x3));
+        x0 = cadd(a, c);
+        x2 = csub(a, c);
+        x1 = cadd(b, d);
+        x3 = csub(b, d);
+        return;
+    }
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 a = __fadd2_rn(x0, x2), b = __ffma2_rn(x2, m1, x0);
+    const float2 c = __fadd2_rn(x1, x3), d = cmul_i<SIGN>(__ffma2_rn(x3, m1, x1));
+    x0 = __fadd2_rn(a, c);
+    x2 = __ffma2_rn(c, m1, a);
     x1 = cadd(b, d);
     x3 = csub(b, d);
 }
@@ -64,13 +78,13 @@ __device__ __forceinline__ float2 w16(int m)
 // 16 = 4 x 4 with twiddles w16^(n1 k1).
 __host__ __device__ constexpr int perm16(int k) { return 4 * (k & 3) + (k >> 2); }
 
-template <int SIGN>
+template <int SIGN, bool kPacked = true>
 __device__ __forceinline__ void dft16(float2 (&x)[16])
 {
     // stage 1: for each n1, 4-point DFT over n2 of x[n1 + 4 n2] -> T[n1][k1] at x[n1 + 4 k1]
 #pragma unroll
     for (int n1 = 0; n1 < 4; n1++)
-        dft4<SIGN>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
+        dft4<SIGN, kPacked>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
     // twiddle by w16^(n1 k1)
 #pragma unroll
     for (int n1 = 1; n1 < 4; n1++)
@@ -80,7 +94,7 @@ __device__ __forceinline__ void dft16(float2 (&x)[16])
     // stage 2: for each k1, 4-point DFT over n1 of x[4 k1 + n1] -> X[k1 + 4 k2] at x[4 k1 + k2]
 #pragma unroll
     for (int k1 = 0; k1 < 4; k1++)
-        dft4<SIGN>(x[4 * k1 + 0], x[4 * k1 + 1], x[4 * k1 + 2], x[4 * k1 + 3]);
+        dft4<SIGN, kPacked>(x[4 * k1 + 0], x[4 * k1 + 1], x[4 * k1 + 2], x[4 * k1 + 3]);
 }
 
 // 256-point complex FFT over a group of 16 threads (thread l = 0..15).
@@ -89,11 +103,11 @@ __device__ __forceinline__ void dft16(float2 (&x)[16])
 // ws: this group's workspace of kPairStride float2; tw: e^(-2 pi i e / 256),
 // e = 0..255 (forward twiddles; the inverse conjugates them).
 // Every thread of the group must call; mask = the group's lanes.
-template <int SIGN>
+template <int SIGN, bool kPacked = true>
 __device__ __forceinline__ void fft256_group(float2 (&x)[16], float2* ws, const float2* tw, int l,
                                              unsigned mask)
 {
-    dft16<SIGN>(x);
+    dft16<SIGN, kPacked>(x);
     // twiddle w256^(SIGN l j) of output j
 #pragma unroll
     for (int j = 1; j < 16; j++) {
@@ -111,7 +125,7 @@ __device__ __forceinline__ void fft256_group(float2 (&x)[16], float2* ws, const 
     for (int n = 0; n < 16; n++)
         x[n] = ws[n * 17 + l];
     __syncwarp(mask);
-    dft16<SIGN>(x);
+    dft16<SIGN, kPacked>(x);
 }
 
 // The same FFT with this thread's twiddles precomputed: twl[j] = the factor

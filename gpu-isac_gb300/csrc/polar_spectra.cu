@@ -172,7 +172,7 @@ polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const f
             x[m] = make_float2(va, vb);
         }
         __syncwarp(gmask); // the pair's samples are read before its region turns workspace
-        fft256_group<-1>(x, gws, tw, l, gmask);
+        fft256_group<-1, false>(x, gws, tw, l, gmask);
         // natural-order spectrum Z[l + 16 k2] to the workspace
 #pragma unroll
         for (int k2 = 0; k2 < 16; k2++)
