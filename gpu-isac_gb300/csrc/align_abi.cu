@@ -357,9 +357,12 @@ enum { K_SPECTRA = 0, K_CCF = 1, K_MMA = 2, K_ZFFT = 3 };
 // variable GPUISAC_CONTRACTION=bf16x3 selects the latter at load time, so an
 // unchanged caller of the reference's entry points can opt in.
 std::atomic<int> g_contraction{-1};
+thread_local int t_contraction_forced = -1;
 
 int contraction_mode()
 {
+    if (t_contraction_forced >= 0)
+        return t_contraction_forced;
     int m = g_contraction.load();
     if (m < 0) {
         const char* e = getenv("GPUISAC_CONTRACTION");
@@ -702,6 +705,8 @@ void clear_state(State& s)
 
 namespace gpuisac {
 
+void contraction_force(int mode) { t_contraction_forced = mode; }
+
 int host_geometry(const AlignConfig* cfg, HostGeometry& out)
 {
     Geometry g;
@@ -991,12 +996,22 @@ int gpuisac_set_contraction(int mode)
         return -1;
     }
     std::lock_guard<std::mutex> lk(g_api_mu);
+    const int forced = t_contraction_forced;
+    t_contraction_forced = -1;
     const int prev = contraction_mode();
+    t_contraction_forced = forced;
     g_contraction.store(mode);
     return prev;
 }
 
-int gpuisac_get_contraction(void) { return contraction_mode(); }
+int gpuisac_get_contraction(void)
+{
+    const int forced = t_contraction_forced;
+    t_contraction_forced = -1;
+    const int m = contraction_mode();
+    t_contraction_forced = forced;
+    return m;
+}
 
 int gpuisac_split_plan(unsigned int ring_num, unsigned int n_shift, unsigned int n_ref, unsigned int* fields,
                        unsigned int n_fields)

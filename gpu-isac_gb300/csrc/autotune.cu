@@ -64,6 +64,7 @@ extern "C" int gpuisac_autotune_ccf(const AlignConfig* cfg, const float* sbj, co
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto cleanup = [&]() {
         ccf_tile_force(nullptr);
+        contraction_force(-1);
         if (d)
             cudaFree(d);
         if (pk)
@@ -96,6 +97,9 @@ extern "C" int gpuisac_autotune_ccf(const AlignConfig* cfg, const float* sbj, co
     std::string rep;
     float best_ms = 1e30f;
     CcfTile best = cand[0];
+    // the candidates are tile shapes of the FP32 CCF kernels: time them with
+    // that contraction whatever the process-wide mode
+    contraction_force(GPUISAC_CONTRACTION_FP32);
     for (size_t i = 0; i < cand.size(); i++) {
         ccf_tile_force(&cand[i]);
         float ms = 1e30f;

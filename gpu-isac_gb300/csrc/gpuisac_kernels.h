@@ -166,6 +166,11 @@ struct CcfWork {
     unsigned wait_iters;
 };
 
+// the contraction the next alignment calls of this thread use regardless of
+// the process-wide mode (the autotuner times FP32 tile shapes this way);
+// -1 clears
+void contraction_force(int mode);
+
 // the failure-path test settings every CCF launch carries (both 0 normally)
 void ccf_test_settings(unsigned& stall, unsigned& wait_iters);
 
