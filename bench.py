@@ -416,7 +416,8 @@ def bench_grouped(args, dev, L, parts_d, refs_d):
     launches = (L.gpuisac_launch_count() - launches0) / (max(args.warmup, 1) + args.steps)
 
     def sequential():
-        return [multi_ref_align_device(parts_d[so:so + n], refs_d[ro:ro + r], NR, s, s) for so, n, ro, r in groups]
+        return [multi_ref_align_device(parts_d[so:so + n], refs_d[ro:ro + r], NR, s, s, contraction_mode="fp32")
+                for so, n, ro, r in groups]
 
     seq, ms_s = timed(sequential, 1, 1)
     same = 0
