@@ -276,27 +276,33 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
                 const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + buf * kAccStride;
                 // Z[k] (a rows) and Z[256 - k] (b rows); slot 0: Z[0], Z[128]
                 const size_t zoff = (size_t)(is_b ? (k ? kRingLen - k : kSlots) : k) * w.zw;
+                // a row: u = sum u a, v = sum v a; b row: u = sum u b, v = sum v b.
+                // The a row writes Z[k] = (sum u a, sum u b), the b row
+                // Z[256-k] = (sum v b, sum v a): each needs one value of its
+                // partner lane, so one shuffle per reference carries it (the
+                // b row sends u, the a row sends v); slot 0, whose (F[0],
+                // F[128]) products combine all four sums, exchanges both.
+                float2* const zrow = zbase + zoff;
                 auto write_chunk = [&](const float (&r)[16], unsigned c) {
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const float u = r[2 * j], v = r[2 * j + 1];
-                        const float pu = __shfl_xor_sync(0xffffffffu, u, 1);
-                        const float pv = __shfl_xor_sync(0xffffffffu, v, 1);
-                        // a row: u = sum u a, v = sum v a; b row: u = sum u b, v = sum v b
-                        const float a1 = is_b ? pu : u, a4 = is_b ? pv : v;
-                        const float a2 = is_b ? u : pu, a3 = is_b ? v : pv;
-                        const unsigned ql = 8 * c + j;
-                        if (row_ok && ql < nq) {
-                            float2 zv;
-                            if (k == 0) {
-                                const float p1 = 0.25f * (a1 + a2 + a3 + a4);
-                                const float p2 = 0.25f * (a1 - a2 + a3 - a4);
-                                zv = is_b ? make_float2(p2, p2) : make_float2(p1, p1);
-                            } else {
-                                zv = is_b ? make_float2(a3, a4) : make_float2(a1, a2);
-                            }
-                            __stcs(zbase + ql * zq + zoff, zv); // streamed: read back only by the next kernel
+                        float2 zv;
+                        if (k == 0) {
+                            const float pu = __shfl_xor_sync(0xffffffffu, u, 1);
+                            const float pv = __shfl_xor_sync(0xffffffffu, v, 1);
+                            const float a1 = is_b ? pu : u, a4 = is_b ? pv : v;
+                            const float a2 = is_b ? u : pu, a3 = is_b ? v : pv;
+                            const float p1 = 0.25f * (a1 + a2 + a3 + a4);
+                            const float p2 = 0.25f * (a1 - a2 + a3 - a4);
+                            zv = is_b ? make_float2(p2, p2) : make_float2(p1, p1);
+                        } else {
+                            const float other = __shfl_xor_sync(0xffffffffu, is_b ? u : v, 1);
+                            zv = make_float2(is_b ? v : u, other);
                         }
+                        const unsigned ql = 8 * c + j;
+                        if (row_ok && ql < nq)
+                            __stcs(zrow + ql * zq, zv); // streamed: read back only by the next kernel
                     }
                 };
                 if (nj) {

@@ -129,6 +129,18 @@ void ref_free_alignment_2D_filter_references(float cutoff_freq, float falloff);
  * host array out.  Returns 0 or an error code. */
 int gpuisac_ref_free_averages(float *out);
 
+/* Replaces the caller-side "normalize.mask" processing of every image before
+ * each alignment call (bin/sp_isac2_gpu.py:925-931; the processor itself is
+ * EMAN2's, not part of the reference tree): for each of the n_img device
+ * images [img_dim][img_dim] in imgs, in place, the mean (and, unless
+ * no_sigma, the population standard deviation) of the pixels where the
+ * device mask [img_dim][img_dim] exceeds 0.5, then x <- (x - mean) / sigma
+ * (x <- x - mean with no_sigma, or when the masked pixels have no spread).
+ * References take no_sigma = 1, particles no_sigma = 0, as the caller does.
+ * Asynchronous on stream.  Returns 0 or an error code. */
+int gpuisac_normalize_mask(float *imgs, unsigned int n_img, unsigned int img_dim, const float *mask, int no_sigma,
+                           void *stream);
+
 /* ---- additions of this library (no counterpart in the reference, which
  * prints and exits on any CUDA error, cuda/gpu_aln_common.cu:104-118) ---- */
 

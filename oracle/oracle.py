@@ -338,3 +338,37 @@ def tanl_filter_averages(avg, cutoff: float, falloff: float) -> np.ndarray:
     out[0] /= n
     out[1:] *= n
     return out
+
+
+def normalize_mask(imgs, mask, no_sigma: bool) -> np.ndarray:
+    """The caller-side masked normalisation before each alignment call
+    (bin/sp_isac2_gpu.py:925-931, EMAN2's "normalize.mask" processor, restated
+    from its published description; EMAN2 is not in the reference tree, so
+    parity with it is unpinned): per image, the mean and population standard
+    deviation (FP64) of the pixels where mask > 0.5; x <- (x - mean) / sigma,
+    or x <- x - mean with no_sigma or when sigma is 0."""
+    x = np.asarray(imgs, np.float64)
+    sel = np.asarray(mask) > 0.5
+    v = x[:, sel]
+    n = max(int(sel.sum()), 1)
+    mean = v.sum(1) / n
+    var = (v * v).sum(1) / n - mean * mean
+    sd = np.sqrt(np.maximum(var, 0.0))
+    out = x - mean[:, None, None]
+    if not no_sigma:
+        ok = sd > 0
+        out[ok] /= sd[ok][:, None, None]
+    return out
+
+
+def ormq_post(peak, base=None):
+    """The caller's conversion of the peak parameters (bin/sp_isac2_gpu.py:
+    1015-1022, the end of ormq() in bin/sp_isac_alignment.py:443-447): the
+    negated shift rotated by the negated angle.  peak [..., 4] = (angle, sx,
+    sy, mirror) with sx, sy relative to the search centre.  Returns (ang,
+    sxs, sys, mirror) in FP64."""
+    peak = np.asarray(peak, np.float64)
+    ang = peak[..., 0]
+    sxn, syn = -peak[..., 1], -peak[..., 2]
+    c, s = np.cos(np.radians(ang)), -np.sin(np.radians(ang))
+    return ang, sxn * c - syn * s, sxn * s + syn * c, peak[..., 3]
