@@ -243,7 +243,10 @@ def bench_reference(args):
 
 
 LEARNED = dict(workload="learned_100000x76_500ref", synth_idx=3, particles=100000, refs=500, train_alignments=200000,
-               img_dim=76, rings=35, shift_range=3, n_shifts=49, snr=0.05, k=32, max_wrong=3e-3)
+               img_dim=76, rings=35, shift_range=3, n_shifts=49, snr=0.05, k=32, max_wrong=3e-3, nk=16)
+# the same workload with the proposal as the workload text writes it: 64
+# harmonics per ring, top-8 references (angles: see bench_learned)
+LEARNED_AS_WRITTEN = dict(LEARNED, workload="learned_100000x76_500ref_as_written_64harm_top8", k=8, nk=64)
 # the headline workload with the learned proposal in front: the chosen form
 # (evaluation particles = the workload's own, training particles an
 # independent draw of the same generator)
@@ -285,7 +288,7 @@ def fp64_check(L, parts, refs, NR, s, best_ref, best_peak):
             "oracle_seconds": t}
 
 
-def bench_learned(args, dev, L, spec=None):
+def bench_learned(args, dev, L, spec=None, resident=None):
     """The learned search against the plain FP32 full search on the learned
     workload: 100,000 held-out particles x 500 references, the network
     trained (untimed) on 200,000 particles the full search labelled.  Both
@@ -296,22 +299,31 @@ def bench_learned(args, dev, L, spec=None):
     from gpuisac import learned, synth
     from gpuisac.align import multi_ref_align_device
     w = spec or LEARNED
-    P = args.learned_particles if spec is None else (w["particles"] or args.particles)
-    n_train = args.learned_train if spec is None else (args.learned_train_largebox or w["train_alignments"])
+    if w["synth_idx"] == LEARNED["synth_idx"]:
+        P, n_train = args.learned_particles, args.learned_train
+    else:
+        P, n_train = (w["particles"] or args.particles), (args.learned_train_largebox or w["train_alignments"])
     R, NR, s = w["refs"], w["rings"], float(w["shift_range"])
     t0 = time.perf_counter()
     tr = synth.workload_stack(w["synth_idx"], n_particles=n_train, n_refs=R, split=1)
-    ev = synth.workload_stack(w["synth_idx"], n_particles=P, n_refs=R)
-    t_gen = time.perf_counter() - t0
-    refs = torch.from_numpy(tr.refs).to(dev)
-    tp = torch.from_numpy(tr.particles).to(dev)
-    ep = torch.from_numpy(ev.particles).to(dev)
     n_chk = min(args.fp64_sample, P)
-    chk_parts, chk_refs = ev.particles[:n_chk].copy(), tr.refs.copy()
-    del tr, ev
+    if resident is not None and resident[1].shape[0] == P:
+        # the evaluation particles are the workload's own, already resident
+        # (the same generator and seed)
+        ev_np, ep, refs = resident
+        chk_parts, chk_refs = ev_np.particles[:n_chk].copy(), ev_np.refs.copy()
+    else:
+        ev = synth.workload_stack(w["synth_idx"], n_particles=P, n_refs=R)
+        ep = torch.from_numpy(ev.particles).to(dev)
+        refs = torch.from_numpy(tr.refs).to(dev)
+        chk_parts, chk_refs = ev.particles[:n_chk].copy(), tr.refs.copy()
+        del ev
+    t_gen = time.perf_counter() - t0
+    tp = torch.from_numpy(tr.particles).to(dev)
+    del tr
     t0 = time.perf_counter()
     d_tr, pk_tr = multi_ref_align_device(tp, refs, NR, s, s, contraction_mode="fp32")
-    net = learned.ProposalNet(NR, device=dev, seed=11)
+    net = learned.ProposalNet(NR, nk=w.get("nk", learned.NK), device=dev, seed=11)
     rep = learned.train_from_full_search(net, tp, refs, d_tr, pk_tr, NR, s, s, k=w["k"], calib_frac=0.1,
                                          max_wrong=w["max_wrong"])
     torch.cuda.synchronize()
@@ -358,7 +370,8 @@ def bench_learned(args, dev, L, spec=None):
             "same_best_ref": float(same.mean()), "same_ref_angle_shift_mirror": float(same_all.mean()),
             "max_rel_peak_err_vs_plain_fp32": float(peak_err.max()),
             "fallback_rate": float(res.fallback.float().mean().item()),
-            "alignments_run_fraction": res.pairs / (P * R), "k": w["k"], "gap_margin": rep.gap_margin,
+            "alignments_run_fraction": res.pairs / (P * R), "k": w["k"], "harmonics": net.nk,
+            "gap_margin": rep.gap_margin,
             "calibration": {"recall_top_k": rep.recall, "fallback_rate": rep.fallback_rate,
                             "max_wrong": w["max_wrong"]},
             "train": {"particles": n_train, "seconds_incl_labelling": t_train, "loss_first_last":
@@ -374,65 +387,179 @@ GROUPED = dict(workload="groups_400_loguniform_100_5000_x76_10to60ref", n_groups
 
 
 def bench_grouped(args, dev, L, parts_d, refs_d):
-    """400 independent groups in one persistent, graph-captured launch
-    sequence (gpuisac_multi_ref_align_groups_device) against the same groups
-    run one call each; tile shape from the autotuner.  Group sizes are
-    log-uniform in [100, 5000] particles with 10..60 references each, cut
-    from the 50,000-particle / 200-reference stacks already resident (groups
-    may overlap in the pool; each is its own stack)."""
+    """400 independent groups per call through gpuisac_multi_ref_align_groups_device
+    (one texture fill, then a spectra and a CCF launch per wave, all reading
+    device tables; the launch graph recorded once per shape), tile shape from
+    the autotuner.  Group sizes are log-uniform in [100, 5000] particles with
+    10..60 references each, cut from the 50,000-particle / 200-reference
+    stacks already resident (groups may overlap in the pool; each is its own
+    stack).  Two such group sets A and B alternate in the timed calls, so that
+    every timed call has other groups than the call before it (its tables and
+    texture objects are rebuilt; the recorded graph is replayed).  Also timed:
+    the first call of the process (recording the graph), both sets as one
+    call per group, and the plain path on the same work mix (one call,
+    every particle of the pool against the groups' mean reference count)."""
     import torch
 
-    from gpuisac.align import ccf_tile_name, multi_ref_align_device, multi_ref_align_groups_device
+    from gpuisac.align import (ccf_tile_name, groups_stats, multi_ref_align_device,
+                               multi_ref_align_groups_device)
     g = GROUPED
     P, R = parts_d.shape[0], refs_d.shape[0]
-    rng = np.random.Generator(np.random.PCG64(20261203 + 2))
-    sizes = np.exp(rng.uniform(np.log(g["min_size"]), np.log(g["max_size"]), g["n_groups"])).astype(int)
-    nrefs = rng.integers(g["min_refs"], g["max_refs"] + 1, g["n_groups"])
-    groups = []
-    for n, r in zip(sizes, nrefs):
-        so = int(rng.integers(0, P - n + 1))
-        ro = int(rng.integers(0, R - r + 1))
-        groups.append((so, int(n), ro, int(r)))
-    alignments = int(sum(n * r for _, n, _, r in groups))
     NR, s = g["rings"], float(g["shift_range"])
     stream = torch.cuda.current_stream(dev)
 
-    def timed(fn, warm, steps):
-        for _ in range(warm):
-            fn()
+    def make_groups(seed):
+        rng = np.random.Generator(np.random.PCG64(seed))
+        sizes = np.exp(rng.uniform(np.log(g["min_size"]), np.log(g["max_size"]), g["n_groups"])).astype(int)
+        nrefs = rng.integers(g["min_refs"], g["max_refs"] + 1, g["n_groups"])
+        out = []
+        for n, r in zip(sizes, nrefs):
+            out.append((int(rng.integers(0, P - n + 1)), int(n), int(rng.integers(0, R - r + 1)), int(r)))
+        return out
+
+    sets = [make_groups(20261203 + 2), make_groups(20261203 + 3)]
+    work = [int(sum(n * r for _, n, _, r in gs)) for gs in sets]
+
+    def run(i):
+        return multi_ref_align_groups_device(parts_d, refs_d, sets[i], NR, s, s)
+
+    # the first call of the process for this shape records the graph
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    first = run(0)
+    torch.cuda.synchronize()
+    first_ms = (time.perf_counter() - t0) * 1000.0
+    first_stats = groups_stats()
+    outs = [first, None]
+    for _ in range(max(args.warmup, 3)):
+        for i in (1, 0):
+            outs[i] = run(i)
+    torch.cuda.synchronize()
+    steps = max(args.steps, 2)
+    launches0 = L.gpuisac_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    done = 0
+    recorded = 0
+    plan_ms = []
+    for k in range(steps):
+        i = (k + 1) % 2  # B, A, B, ...: each call's groups differ from the previous call's
+        outs[i] = run(i)
+        st_k = groups_stats()
+        recorded += int(st_k["graph_recorded"])
+        plan_ms.append(st_k["plan_ms"])
+        done += work[i]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t0) * 1000.0
+    ms_g = e0.elapsed_time(e1) / steps
+    launches = (L.gpuisac_launch_count() - launches0) / steps
+    stats = groups_stats()
+
+    def sequential(i):
+        return [multi_ref_align_device(parts_d[so:so + n], refs_d[ro:ro + r], NR, s, s, contraction_mode="fp32")
+                for so, n, ro, r in sets[i]]
+
+    same, seq_ms = [], []
+    for i in (0, 1):
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        out = None
-        for _ in range(steps):
-            out = fn()
+        seq = sequential(i)
         e1.record(stream)
         torch.cuda.synchronize()
-        return out, e0.elapsed_time(e1) / steps
+        seq_ms.append(e0.elapsed_time(e1))
+        dg, pg, offs = outs[i]
+        dg_h, pg_h = dg.cpu().numpy(), pg.cpu().numpy()
+        n_same = 0
+        for (so, n, ro, r), off, (d1, p1) in zip(sets[i], offs, seq):
+            n_same += int(np.array_equal(dg_h[off:off + n * r].reshape(r, n), d1.cpu().numpy()) and
+                          np.array_equal(pg_h[off:off + n * r].reshape(r, n, 4), p1.cpu().numpy()))
+        same.append(n_same)
+        del seq
 
-    launches0 = L.gpuisac_launch_count()
-    (dg, pg, offs), ms_g = timed(lambda: multi_ref_align_groups_device(parts_d, refs_d, groups, NR, s, s),
-                                 max(args.warmup, 1), args.steps)
-    launches = (L.gpuisac_launch_count() - launches0) / (max(args.warmup, 1) + args.steps)
-
-    def sequential():
-        return [multi_ref_align_device(parts_d[so:so + n], refs_d[ro:ro + r], NR, s, s, contraction_mode="fp32")
-                for so, n, ro, r in groups]
-
-    seq, ms_s = timed(sequential, 1, 1)
-    same = 0
-    dg_h, pg_h = dg.cpu().numpy(), pg.cpu().numpy()
-    for (so, n, ro, r), off, (d1, p1) in zip(groups, offs, seq):
-        same += int(np.array_equal(dg_h[off:off + n * r].reshape(r, n), d1.cpu().numpy()) and
-                    np.array_equal(pg_h[off:off + n * r].reshape(r, n, 4), p1.cpu().numpy()))
-    return {"workload": g["workload"], "value": alignments / (ms_g / 1000.0), "unit": UNIT, "ms_per_step": ms_g,
-            "steps": args.steps, "warmup": max(args.warmup, 1), "alignments_per_step": alignments,
-            "particles_per_step": int(sizes.sum()),
-            "sequential_per_group_calls": {"value": alignments / (ms_s / 1000.0), "ms": ms_s},
-            "groups_identical_to_sequential": f"{same}/{len(groups)}",
+    # the plain path on the same work mix: every particle of the pool against
+    # the groups' mean reference count (one call)
+    r_mix = int(round(sum(work) / sum(sum(n for _, n, _, _ in gs) for gs in sets)))
+    for _ in range(2):
+        multi_ref_align_device(parts_d, refs_d[:r_mix], NR, s, s, contraction_mode="fp32")
+    torch.cuda.synchronize()
+    e0.record(stream)
+    multi_ref_align_device(parts_d, refs_d[:r_mix], NR, s, s, contraction_mode="fp32")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mix_ms = e0.elapsed_time(e1)
+    value = done / (ms_g * steps / 1000.0)
+    return {"workload": g["workload"], "value": value, "unit": UNIT, "ms_per_step": ms_g,
+            "steps": steps, "warmup": max(args.warmup, 3),
+            "alignments_per_step": done / steps, "particles_per_call": [int(sum(n for _, n, _, _ in gs)) for gs in sets],
+            "timed_calls": "group sets A and B alternate: every call has other groups than the call before it",
+            "host_wall_ms_per_step": wall_ms / steps,
+            "plan_ms_per_call": float(np.mean(plan_ms)), "graphs_recorded_in_timed_calls": recorded,
+            "first_call": {"ms": first_ms, "record_ms": first_stats["record_ms"], "plan_ms": first_stats["plan_ms"],
+                           "note": "first call of the process: allocations, texture layout, graph recording"},
+            "waves": stats["waves"], "launches_per_call": launches, "graph_launches": stats["graph_launches"],
+            "sequential_per_group_calls": {"value": sum(work) / (sum(seq_ms) / 1000.0), "ms": seq_ms},
+            "groups_identical_to_sequential": f"{sum(same)}/{2 * len(sets[0])}",
+            "plain_same_mix": {"value": P * r_mix / (mix_ms / 1000.0), "ms": mix_ms, "particles": P, "refs": r_mix,
+                               "note": "one plain call, all pool particles x the groups' mean reference count"},
             "tile": ccf_tile_name(NR, g["n_shifts"]),
-            "kernel_launches_per_step_incl_graph_nodes": launches,
             "data": "groups cut from the resident 50k-particle / 200-ref synthetic stacks"}
+
+
+GROUPED_LARGEBOX = dict(workload="largebox_groups_loguniform_500_20000_x128_500ref", min_size=500, max_size=20000,
+                        rings=61, shift_range=4, n_shifts=81, checked_groups=3)
+
+
+def bench_grouped_largebox(args, dev, L, parts_d, refs_d):
+    """The large-box stack cut into consecutive groups of log-uniform size in
+    [500, 20000] particles (the last group takes the rest), every group
+    against all references, in one gpuisac_multi_ref_align_groups_device call
+    per step; a few groups compared bit for bit with their own separate
+    calls."""
+    import torch
+
+    from gpuisac.align import groups_stats, multi_ref_align_device, multi_ref_align_groups_device
+    g = GROUPED_LARGEBOX
+    P, R = parts_d.shape[0], refs_d.shape[0]
+    NR, s = g["rings"], float(g["shift_range"])
+    rng = np.random.Generator(np.random.PCG64(20261203 + 4 + 2))
+    groups, a = [], 0
+    while a < P:
+        n = int(np.exp(rng.uniform(np.log(g["min_size"]), np.log(g["max_size"]))))
+        n = min(n, P - a)
+        groups.append((a, n, 0, R))
+        a += n
+    stream = torch.cuda.current_stream(dev)
+    out = multi_ref_align_groups_device(parts_d, refs_d, groups, NR, s, s)  # first call: records the graph
+    first = groups_stats()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(1, min(args.steps, 2))
+    e0.record(stream)
+    for _ in range(steps):
+        out = multi_ref_align_groups_device(parts_d, refs_d, groups, NR, s, s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    stats = groups_stats()
+    d, pk, offs = out
+    same = 0
+    pick = rng.choice(len(groups), size=min(g["checked_groups"], len(groups)), replace=False)
+    for i in pick:
+        so, n, ro, r = groups[i]
+        d1, p1 = multi_ref_align_device(parts_d[so:so + n], refs_d[ro:ro + r], NR, s, s, contraction_mode="fp32")
+        off = offs[i]
+        same += int(torch.equal(d[off:off + n * r].view(r, n), d1) and
+                    torch.equal(pk[off:off + n * r].view(r, n, 4), p1))
+    del out, d, pk
+    torch.cuda.empty_cache()
+    return {"workload": g["workload"], "value": P * R / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms,
+            "steps": steps, "groups": len(groups), "particles": P, "refs_per_group": R,
+            "waves": stats["waves"], "graph_launches": stats["graph_launches"],
+            "first_call_record_ms": first["record_ms"], "plan_ms": stats["plan_ms"],
+            "groups_identical_to_separate_calls": f"{same}/{len(pick)} (sampled)",
+            "contraction": "fp32 (the grouped launch sequence runs the FP32 CCF kernels)"}
 
 
 def bench_assign(args, dev, L, d_dev, cpu=True):
@@ -985,7 +1112,7 @@ def bench_ours(args):
     # search, on the same particles, against the plain FP32 full search ----
     chosen = None
     if rank == 0 and world == 1 and not args.no_learned and WORKLOAD["workload"].startswith("mref"):
-        blk = bench_learned(args, dev, L, LEARNED_MREF)
+        blk = bench_learned(args, dev, L, LEARNED_MREF, resident=(st, parts_d, refs_d))
         chosen = {"form": "learned reference proposal (network inference on the tensor cores, top-32 references) "
                           "+ exhaustive shift x angle x mirror search of every proposal, full search of every "
                           "reference below the calibrated margin",
@@ -1019,10 +1146,22 @@ def bench_ours(args):
         grouped_blk = bench_grouped(args, dev, L, parts_d, refs_d)
     if rank == 0 and world == 1 and not args.no_cpu:
         prec = precision_vs_fp64(dev, n=256 if WORKLOAD["workload"].startswith("mref") else 32)
+    if rank == 0 and world == 1 and WORKLOAD["workload"].startswith("largebox") and not args.no_grouped_largebox:
+        grouped_blk = bench_grouped_largebox(args, dev, L, parts_d, refs_d)
     if rank == 0 and world == 1 and not args.no_learned:
-        del parts_d
-        torch.cuda.empty_cache()
-        learned_blk = bench_learned(args, dev, L, learned_spec)
+        if learned_spec is None:
+            del parts_d
+            torch.cuda.empty_cache()
+            learned_blk = bench_learned(args, dev, L, learned_spec)
+        else:
+            learned_blk = bench_learned(args, dev, L, learned_spec, resident=(st, parts_d, refs_d))
+        if learned_spec is None and not args.no_learned_as_written:
+            torch.cuda.empty_cache()
+            aw = bench_learned(args, dev, L, LEARNED_AS_WRITTEN)
+            aw["coarse_angles"] = ("not proposed: one inverse FFT gives every one of the 256 angles of a "
+                                   "(shift, reference) pair, so the search of each proposed reference covers "
+                                   "the top-16 coarse angles and their neighbourhoods at no extra cost")
+            learned_blk = {"chosen_16harm_top32": learned_blk, "as_written_64harm_top8": aw}
 
     if rank == 0:
         dtype = "bf16x3 (BF16 hi/lo split operands, FP32 accumulate)" if args.contraction == "bf16x3" else "f32"
@@ -1033,7 +1172,8 @@ def bench_ours(args):
                 "config": dict(WORKLOAD, particles=P, autotune=tune,
                                path="plain FP32 CUDA-core contraction" if args.contraction == "fp32" else
                                "BF16 hi/lo split contraction on the tensor cores (tcgen05), pair spectra through HBM",
-                               l2="inputs (1.16 GB images, spectra chunks of GBs) exceed the 129 MB L2"),
+                               l2=f"inputs ({P * w['img_dim'] ** 2 * 4 / 1e9:.2f} GB images, spectra or operand "
+                                  "chunks of GBs) exceed the 129 MB L2"),
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "split_kernels": split_ms if args.contraction == "bf16x3" else None,
                 "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk,
@@ -1064,6 +1204,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-search comparison")
     ap.add_argument("--no-grouped", action="store_true", help="skip the grouped-launch comparison")
+    ap.add_argument("--no-grouped-largebox", action="store_true",
+                    help="largebox: skip the batched uneven groups over the whole stack")
+    ap.add_argument("--no-learned-as-written", action="store_true",
+                    help="skip the learned proposal as the workload writes it (64 harmonics, top-8)")
     ap.add_argument("--no-assign", action="store_true", help="skip the group-assignment block")
     ap.add_argument("--no-multigroup", action="store_true", help="skip the multigroup (stability test) block")
     ap.add_argument("--no-prealign", action="store_true", help="skip the pre-alignment block")

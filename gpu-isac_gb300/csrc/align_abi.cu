@@ -105,7 +105,9 @@ std::vector<float2> polar_template(unsigned ring_num, unsigned ring_len)
     return t;
 }
 
-int validate(const AlignConfig* cfg, Geometry& g, bool need_type)
+// ring_len: 256 everywhere; 512 where allow_l512 (the multi-reference calls,
+// ring512.cu)
+int validate(const AlignConfig* cfg, Geometry& g, bool need_type, bool allow_l512 = false)
 {
     if (!cfg) {
         set_error(E_ARG, "AlignConfig is NULL");
@@ -115,8 +117,9 @@ int validate(const AlignConfig* cfg, Geometry& g, bool need_type)
         set_error(E_UNSUPPORTED, "aln_type '%s' is not the multi-reference path ('mref_aln')", cfg->aln_type);
         return E_UNSUPPORTED;
     }
-    if (cfg->ring_len != (unsigned)kRingLen) {
-        set_error(E_UNSUPPORTED, "ring_len %u unsupported (this library computes 256-sample rings)", cfg->ring_len);
+    if (cfg->ring_len != (unsigned)kRingLen && !(allow_l512 && cfg->ring_len == (unsigned)kRingLen512)) {
+        set_error(E_UNSUPPORTED, "ring_len %u unsupported (256-sample rings%s)", cfg->ring_len,
+                  allow_l512 ? "; 512 on the multi-reference path" : " on this entry point");
         return E_UNSUPPORTED;
     }
     if (cfg->ring_num == 0 || cfg->ring_num > kMaxRingNum) {
@@ -213,9 +216,9 @@ struct DevBuf {
 
 struct Workspace {
     // geometry currently uploaded (skip re-uploading an unchanged one)
-    unsigned geo_D = 0, geo_NR = 0;
+    unsigned geo_D = 0, geo_NR = 0, geo_L = 0;
     std::vector<float2> geo_shifts;
-    DevBuf<float2> tmpl, tw, shifts_f, ref_sp, sbj_sp, base;
+    DevBuf<float2> tmpl, tw, tw512, shifts_f, ref_sp, sbj_sp, base;
     DevBuf<int2> shifts_i, zero_shift;
     DevBuf<unsigned> err; // device-side timeout flag of the kernels' bounded waits
     DevBuf<unsigned char> sop, rop; // BF16 hi/lo operands of the tensor-core contraction
@@ -239,11 +242,12 @@ struct Workspace {
         zsp.release();
         ref_tex.release();
         sbj_tex.release();
-        geo_D = geo_NR = 0;
+        geo_D = geo_NR = geo_L = 0;
         geo_shifts.clear();
         zero_shift.release();
         tmpl.release();
         tw.release();
+        tw512.release();
         shifts_f.release();
         ref_sp.release();
         sbj_sp.release();
@@ -252,12 +256,12 @@ struct Workspace {
     }
 };
 
-// forward twiddles e^(-2 pi i e / 256), computed in double
-std::vector<float2> twiddles()
+// forward twiddles e^(-2 pi i e / n), computed in double
+std::vector<float2> twiddles(int n = kRingLen)
 {
-    std::vector<float2> t(kRingLen);
-    for (int e = 0; e < kRingLen; e++) {
-        double a = -2.0 * M_PI * (double)e / (double)kRingLen;
+    std::vector<float2> t(n);
+    for (int e = 0; e < n; e++) {
+        double a = -2.0 * M_PI * (double)e / (double)n;
         t[e] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
     return t;
@@ -265,13 +269,14 @@ std::vector<float2> twiddles()
 
 int upload_geometry(const Geometry& g, Workspace& ws, cudaStream_t st)
 {
-    if (ws.geo_D == g.D && ws.geo_NR == g.NR && ws.geo_shifts.size() == g.shifts_f.size() && ws.tmpl.p &&
-        std::memcmp(ws.geo_shifts.data(), g.shifts_f.data(), g.shifts_f.size() * sizeof(float2)) == 0)
+    if (ws.geo_D == g.D && ws.geo_NR == g.NR && ws.geo_L == g.L && ws.geo_shifts.size() == g.shifts_f.size() &&
+        ws.tmpl.p && std::memcmp(ws.geo_shifts.data(), g.shifts_f.data(), g.shifts_f.size() * sizeof(float2)) == 0)
         return 0;
-    if (ws.tmpl.ensure(g.tmpl.size()) || ws.tw.ensure(kRingLen) || ws.shifts_f.ensure(g.S) ||
-        ws.shifts_i.ensure(g.S) || ws.zero_shift.ensure(1))
+    if (ws.tmpl.ensure(g.tmpl.size()) || ws.tw.ensure(kRingLen) || ws.tw512.ensure(kRingLen512) ||
+        ws.shifts_f.ensure(g.S) || ws.shifts_i.ensure(g.S) || ws.zero_shift.ensure(1))
         return E_NOMEM;
-    std::vector<float2> tw = twiddles();
+    std::vector<float2> tw = twiddles(), tw512 = twiddles(kRingLen512);
+    CK(cudaMemcpyAsync(ws.tw512.p, tw512.data(), tw512.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
     const int2 zero = make_int2(0, 0);
     CK(cudaMemcpyAsync(ws.zero_shift.p, &zero, sizeof(int2), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(ws.tmpl.p, g.tmpl.data(), g.tmpl.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
@@ -282,6 +287,7 @@ int upload_geometry(const Geometry& g, Workspace& ws, cudaStream_t st)
     CK(cudaStreamSynchronize(st));
     ws.geo_D = g.D;
     ws.geo_NR = g.NR;
+    ws.geo_L = g.L;
     ws.geo_shifts = g.shifts_f;
     return 0;
 }
@@ -484,6 +490,48 @@ int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs,
 // Device-resident multi-reference alignment of P particles against R refs.
 // With host destinations, each chunk's columns are copied back on a second
 // stream while the next chunk computes.
+// 512-sample rings (ring512.cu): FP32 contraction whatever the mode; chunks
+// of particles bounded by the memory request, results copied to the host at
+// the end when `host` is given
+int run_alignment_l512(const Geometry& g, Workspace& ws, const StackDesc& refs, const StackDesc& sbjs,
+                       const unsigned long long* ref_tx, const unsigned long long* sbj_tx, const float2* d_base,
+                       float* d_out, float4* d_peak, float mem_request, cudaStream_t st, const HostOut* host)
+{
+    const size_t row_elems = (size_t)g.NR * kSlots512;
+    if (ws.ref_sp.ensure(row_elems * std::max(g.R, 1u)))
+        return E_NOMEM;
+    cudaEvent_t ev = g_timer.begin(st);
+    CK(launch_polar_spectra512(refs, ws.tmpl.p, ws.tw512.p, g.NR, ws.zero_shift.p, 1, nullptr, 0, g.R, 1,
+                               ws.ref_sp.p, st, ref_tx));
+    g_timer.end(K_SPECTRA, ev, st);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const double frac = (mem_request > 0.f && mem_request <= 1.f) ? mem_request : 0.9;
+    const size_t budget = (size_t)((double)free_b * frac) / 2;
+    const size_t per_part = row_elems * g.S * sizeof(float2);
+    const size_t chunk = std::min<size_t>(std::max<size_t>(1, std::min<size_t>(budget / per_part, 2048)), g.P);
+    if (ws.sbj_sp.ensure(per_part / sizeof(float2) * chunk))
+        return E_NOMEM;
+    for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk) {
+        const unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
+        ev = g_timer.begin(st);
+        CK(launch_polar_spectra512(sbjs, ws.tmpl.p, ws.tw512.p, g.NR, ws.shifts_i.p, g.S, d_base, p0, n, 0,
+                                   ws.sbj_sp.p, st, sbj_tx));
+        g_timer.end(K_SPECTRA, ev, st);
+        ev = g_timer.begin(st);
+        CK(launch_ccf_peak512(ws.sbj_sp.p, ws.ref_sp.p, ws.tw512.p, g.NR, g.S, g.R, n, p0, g.P, ws.shifts_f.p, d_base,
+                              d_out, d_peak, st));
+        g_timer.end(K_CCF, ev, st);
+    }
+    if (host) {
+        CK(cudaMemcpy2DAsync(host->d, (size_t)host->d_pitch * sizeof(float), d_out, (size_t)g.P * sizeof(float),
+                             (size_t)g.P * sizeof(float), g.R, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(host->peak, d_peak, (size_t)g.R * g.P * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return 0;
+}
+
 int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, const float* d_sbj, const float* d_ref,
                   const float2* d_base, float* d_out, float4* d_peak, float mem_request, cudaStream_t st,
                   const HostOut* host = nullptr)
@@ -508,6 +556,8 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
         ref_tx = ws.ref_tex.try_build(refs, st);
         sbj_tx = ws.sbj_tex.try_build(sbjs, st);
     }
+    if (g.L == (unsigned)kRingLen512)
+        return run_alignment_l512(g, ws, refs, sbjs, ref_tx, sbj_tx, d_base, d_out, d_peak, mem_request, st, host);
     if (contraction_mode() == GPUISAC_CONTRACTION_BF16X3)
         return run_alignment_split(g, ws, refs, sbjs, ref_tx, sbj_tx, d_base, d_out, d_peak, mem_request, st, host);
     const size_t row_elems = (size_t)g.NR * kSlots; // float2 per (image, shift) row
@@ -767,7 +817,7 @@ AlignParam* multi_ref_align_init(const AlignConfig* aln_cfg, unsigned int cuda_d
         return nullptr;
     }
     Geometry geo;
-    if (validate(aln_cfg, geo, true))
+    if (validate(aln_cfg, geo, true, true))
         return nullptr;
     cudaError_t e = cudaSetDevice((int)cuda_device_id);
     if (e != cudaSuccess) {
@@ -794,11 +844,11 @@ void multi_ref_align(const float** sbj_data, const float** ref_data, float* isac
     // the configuration may have been edited between init and this call
     if (s.cfg) {
         Geometry geo;
-        if (validate(s.cfg, geo, true))
+        if (validate(s.cfg, geo, true, true))
             return;
         s.geo.P = geo.P;
         s.geo.R = geo.R;
-        if (geo.D != s.geo.D || geo.NR != s.geo.NR)
+        if (geo.D != s.geo.D || geo.NR != s.geo.NR || geo.L != s.geo.L)
             s.geo = geo;
     }
     do_multi_ref_align(s, sbj_data, ref_data, isac_peak_list, isac_d, isac_d_pitch, cuda_mem_request);
@@ -884,7 +934,7 @@ int gpuisac_multi_ref_align_device(const AlignConfig* cfg, const float* sbj, con
                                    const float* base_shift, float* d_out, float* peak_out, void* stream)
 {
     Geometry g;
-    int rc = validate(cfg, g, false);
+    int rc = validate(cfg, g, false, true);
     if (rc)
         return rc;
     if (!sbj || !ref || !d_out || !peak_out) {

@@ -28,11 +28,12 @@ __device__ __forceinline__ bool better(float v, unsigned h, unsigned t, float bv
 
 // Reference: angle from the peak index and the 7-point parabola,
 // cuda/gpu_aln_noref.cu:1773-1793 (same float/double mixing).
-__device__ float peak_angle(const float* x, unsigned tau, bool mirror)
+// (ring_len: samples per ring, the reference's cfg->ring_len)
+__device__ float peak_angle(const float* x, unsigned tau, bool mirror, unsigned ring_len = kRingLen)
 {
     float c2 = (float)(49. * x[0] + 6. * x[1] - 21. * x[2] - 32. * x[3] - 27. * x[4] - 6. * x[5] + 31. * x[6]);
     float c3 = (float)(5. * x[0] - 3. * x[2] - 4. * x[3] - 3. * x[4] + 5. * x[6]);
-    float step = (float)(360.0 / (double)(float)kRingLen);
+    float step = (float)(360.0 / (double)(float)ring_len);
     float angle = step * (float)tau;
     if (c3 != 0.0)
         angle = (float)((double)angle + (double)step * ((double)c2 / (2.0 * (double)c3) - 4));

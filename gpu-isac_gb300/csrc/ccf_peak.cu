@@ -58,20 +58,21 @@ __device__ __forceinline__ unsigned ref_row(const CcfGroup& g, unsigned q) { ret
 __device__ __forceinline__ bool decode_item(const CcfWork& w, unsigned item, int qt, CcfGroup& grp, unsigned& q0,
                                             unsigned& pb, unsigned& pe)
 {
-    if (item >= w.n_items)
+    if (item >= (w.dyn ? __ldg(w.dyn + 2) : w.n_items))
         return false;
     if (w.groups == nullptr) {
         grp = w.one;
     } else {
-        unsigned lo = 0, hi = w.n_groups - 1; // last group with item_begin <= item
+        const CcfGroup* groups = w.dyn ? w.groups + __ldg(w.dyn) : w.groups;
+        unsigned lo = 0, hi = (w.dyn ? __ldg(w.dyn + 1) : w.n_groups) - 1; // last group with item_begin <= item
         while (lo < hi) {
             const unsigned mid = (lo + hi + 1) >> 1;
-            if (w.groups[mid].item_begin <= item)
+            if (groups[mid].item_begin <= item)
                 lo = mid;
             else
                 hi = mid - 1;
         }
-        grp = w.groups[lo];
+        grp = groups[lo];
     }
     const unsigned local = item - grp.item_begin;
     const unsigned tile = local % grp.ref_tiles, blk = local / grp.ref_tiles;

@@ -25,10 +25,11 @@
 //                   a/b lanes by shuffle and write Z[k], Z[256-k] of every
 //                   (shift, reference) pair.
 // zfft_peak_kernel  persistent; work item = (particle, reference); the Z block
-//                   of each shift block is bulk-copied into one of two shared
-//                   buffers while the previous one is transformed; 16 threads
-//                   per shift run the inverse FFT and the peak search, the
-//                   shift slots are merged at the particle's end.
+//                   of each shift block is bulk-copied into a shared buffer
+//                   as soon as every 16-thread group has taken its shift's
+//                   column of the previous one, each group running the
+//                   inverse FFT and the peak search in its own workspace; a
+//                   control warp merges the groups' bests at the item's end.
 //
 // Every wait is bounded (about a second); a kernel that gives up sets *err,
 // lets its own copies and MMAs land, frees its tensor memory and returns.
@@ -345,22 +346,40 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
 
 // ============================================================================
 // inverse FFT + peak search of the pair spectra Z, one (particle, reference)
-// per work item, one 16-thread group per shift of a block (up to
-// kSplitMaxBlock = 49 groups, 784 threads)
-template <int RR>
-__global__ void __launch_bounds__(16 * kSplitMaxBlock, 1)
+// per work item, one 16-thread group per shift of a block (w.block groups, up
+// to kSplitMaxBlock = 49, in whole warps), plus one control warp.  The units
+// (item, shift block) stream through one shared Z buffer: the control warp
+// copies unit u + 1 in as soon as every group has taken its unit-u column into
+// registers (mbarrier `empty`), so the copy overlaps the FFTs; each group then
+// transforms in its own workspace and runs on without waiting for the others.
+// A finished item's group bests are parked in one of kZfftRing slot sets
+// (mbarrier `parked`); the control warp merges them, writes the outputs and
+// hands the set back (mbarrier `freed`).
+constexpr int kZfftCtlThreads = 32;
+constexpr unsigned kZfftRing = 4;
+__host__ __device__ constexpr unsigned zfft_group_threads(unsigned groups) { return (16 * groups + 31) / 32 * 32; }
+__host__ __device__ constexpr size_t zfft_zbuf_bytes(unsigned zw)
+{
+    return ((size_t)kRingLen * zw * sizeof(float2) + 15) / 16 * 16;
+}
+
+__global__ void __launch_bounds__(zfft_group_threads(kSplitMaxBlock) + kZfftCtlThreads, 1)
 zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    const unsigned groups = blockDim.x >> 4;
-    const size_t zbuf_bytes = std::max((size_t)kRingLen * w.zw * sizeof(float2),
-                                       (size_t)groups * kPairStride * sizeof(float2));
-    float2* const zb0 = reinterpret_cast<float2*>(smem_raw);
-    float2* const zb1 = reinterpret_cast<float2*>(smem_raw + zbuf_bytes);
-    float2* tw = reinterpret_cast<float2*>(smem_raw + 2 * zbuf_bytes); // [16][kTwRow]
-    PeakSlot* slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);    // [2][64] parked bests of two items
-    uint64_t* full = reinterpret_cast<uint64_t*>(slots + 128);         // [2]
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(full + 2);
+    const unsigned groups = w.block;
+    const unsigned gthreads = 16 * groups;
+    const bool ctl = threadIdx.x >= zfft_group_threads(groups);
+    const size_t unit_elems = (size_t)kRingLen * w.zw;
+    float2* const zb = reinterpret_cast<float2*>(smem_raw);                                // [256][zw]
+    float2* const wsp = reinterpret_cast<float2*>(smem_raw + zfft_zbuf_bytes(w.zw));       // [groups][kPairStride]
+    float2* const tw = wsp + (size_t)groups * kPairStride;                                 // [16][kTwRow]
+    PeakSlot* const slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);                 // [kZfftRing][64]
+    uint64_t* const full = reinterpret_cast<uint64_t*>(slots + kZfftRing * 64);
+    uint64_t* const empty = full + 1;
+    uint64_t* const parked = full + 2;             // [kZfftRing]
+    uint64_t* const freed = parked + kZfftRing;    // [kZfftRing]
+    volatile int* const abort_flag = reinterpret_cast<volatile int*>(freed + kZfftRing);
 
     const int tid = threadIdx.x;
     const unsigned n_items = w.n_part * w.n_ref;
@@ -373,136 +392,160 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
     }
     if (tid == 0) {
         mbar_init(full, 1);
-        mbar_init(full + 1, 1);
+        mbar_init(empty, gthreads);
+        for (unsigned i = 0; i < kZfftRing; i++) {
+            mbar_init(parked + i, gthreads);
+            mbar_init(freed + i, 1);
+        }
         *abort_flag = 0;
         mbar_fence_init();
     }
     __syncthreads();
 
-    const size_t unit_elems = (size_t)kRingLen * w.zw;
     // units of this CTA: (item, block), item = particle x reference
     const unsigned my_items = (n_items - blockIdx.x + gridDim.x - 1) / gridDim.x;
     const unsigned n_units = my_items * w.n_blocks;
     auto unit_item = [&](unsigned u) { return blockIdx.x + (u / w.n_blocks) * gridDim.x; };
     const uint32_t wlim = wait_tries(w.wait_iters);
-    auto issue = [&](unsigned u) {
-        if (w.test_stall)
-            return; // failure-path test: no copies
-        const unsigned item = unit_item(u), b = u % w.n_blocks;
-        const uint32_t bytes = (uint32_t)(unit_elems * sizeof(float2));
-        fence_proxy_async();
-        mbar_expect_tx(full + (u & 1u), bytes);
-        bulk_g2s((u & 1u) ? zb1 : zb0, w.z + ((size_t)item * w.n_blocks + b) * unit_elems, bytes, full + (u & 1u));
-    };
-    if (tid == 0) {
-        issue(0);
-        if (n_units > 1)
-            issue(1);
+
+    if (ctl) {
+        // ---------------- control warp: copies, merges, outputs ----------------
+        const int lane = tid & 31;
+        auto issue = [&](unsigned u) {
+            if (w.test_stall)
+                return; // failure-path test: no copies
+            const unsigned item = unit_item(u), b = u % w.n_blocks;
+            const uint32_t bytes = (uint32_t)(unit_elems * sizeof(float2));
+            fence_proxy_async();
+            mbar_expect_tx(full, bytes);
+            bulk_g2s(zb, w.z + ((size_t)item * w.n_blocks + b) * unit_elems, bytes, full);
+        };
+        // the groups' parked bests of a finished item, reduced in the
+        // reference's order (better(); equal entries: the lower group, which
+        // holds the lower shifts), then the parabola and the outputs
+        auto merge = [&](unsigned item, const PeakSlot* sl) {
+            unsigned bi = (unsigned)lane < groups ? (unsigned)lane : 0u;
+            float v = sl[bi].v;
+            unsigned h = sl[bi].h, t = sl[bi].t;
+            if ((unsigned)lane + 32 < groups) { // up to 64 groups: two per lane
+                const PeakSlot& o = sl[lane + 32];
+                if (better(o.v, o.h, o.t, v, h, t)) {
+                    v = o.v;
+                    h = o.h;
+                    t = o.t;
+                    bi = lane + 32;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const float v2 = __shfl_xor_sync(0xffffffffu, v, off);
+                const unsigned h2 = __shfl_xor_sync(0xffffffffu, h, off), t2 = __shfl_xor_sync(0xffffffffu, t, off);
+                const unsigned b2 = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (better(v2, h2, t2, v, h, t) || (v2 == v && h2 == h && t2 == t && b2 < bi)) {
+                    v = v2;
+                    h = h2;
+                    t = t2;
+                    bi = b2;
+                }
+            }
+            if (lane == 0) {
+                const PeakSlot& ps = sl[bi];
+                const bool mirror = ps.h >= w.n_shift;
+                const unsigned sidx = mirror ? ps.h - w.n_shift : ps.h;
+                const float angle =
+                    w.rule == kPeakPreAlign ? pre_peak_angle(ps.nb, ps.t, mirror) : peak_angle(ps.nb, ps.t, mirror);
+                const unsigned p = item / w.n_ref, q = item - p * w.n_ref;
+                const unsigned pg = w.p_first + p;
+                const float bx = w.base ? w.base[pg].x : 0.f, by = w.base ? w.base[pg].y : 0.f;
+                const float2 sf = w.shifts_f[sidx];
+                const size_t o = (size_t)q * w.p_total + pg;
+                w.d_out[o] = ps.v;
+                w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+            }
+        };
+        bool failed = false;
+        unsigned issued = 0, n_done = 0;
+        if (lane == 0 && n_units > 0)
+            issue(0);
+        issued = n_units > 0 ? 1 : 0;
+        for (unsigned u = 0; u < n_units; u++) {
+            // every group holds its unit-u column: the buffer takes unit u + 1
+            bool ok = true;
+            if (lane == 0) {
+                ok = mbar_wait_abort(empty, u & 1u, abort_flag, wlim);
+                if (ok && u + 1 < n_units)
+                    issue(u + 1);
+            }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                failed = true;
+                break;
+            }
+            if (u + 1 < n_units)
+                issued = u + 2;
+            if (u % w.n_blocks == w.n_blocks - 1) {
+                const unsigned set = n_done % kZfftRing;
+                ok = mbar_wait_abort(parked + set, (n_done / kZfftRing) & 1u, abort_flag, wlim);
+                if (!__all_sync(0xffffffffu, ok)) {
+                    failed = true;
+                    break;
+                }
+                merge(unit_item(u), slots + 64 * set);
+                __syncwarp();
+                if (lane == 0)
+                    mbar_arrive(freed + set);
+                n_done++;
+            }
+        }
+        if (failed && lane == 0) {
+            *abort_flag = 1;
+            atomicExch(err, 1u);
+            // the last copy issued lands before the CTA ends (bounded)
+            if (issued && !w.test_stall)
+                mbar_wait(full, (issued - 1) & 1u, wlim);
+        }
+        return;
     }
 
+    // ---------------- FFT groups ----------------
     const int g = tid >> 4, l = tid & 15;
+    if ((unsigned)g >= groups)
+        return; // the unused half of the last warp
     const unsigned gmask = 0xffffu << (tid & 16);
-    // merge of a finished item by warp 0: the groups' parked bests reduced
-    // with the reference's order (better(); equal entries: the lower group,
-    // which holds the lower shifts), then the parabola and the outputs
-    auto merge = [&](unsigned item, const PeakSlot* sl) {
-        const int lane = tid & 31;
-        unsigned bi = (unsigned)lane < groups ? (unsigned)lane : 0u;
-        float v = sl[bi].v;
-        unsigned h = sl[bi].h, t = sl[bi].t;
-        if ((unsigned)lane + 32 < groups) { // up to 64 groups: two per lane
-            const PeakSlot& o = sl[lane + 32];
-            if (better(o.v, o.h, o.t, v, h, t)) {
-                v = o.v;
-                h = o.h;
-                t = o.t;
-                bi = lane + 32;
-            }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float v2 = __shfl_xor_sync(0xffffffffu, v, off);
-            const unsigned h2 = __shfl_xor_sync(0xffffffffu, h, off), t2 = __shfl_xor_sync(0xffffffffu, t, off);
-            const unsigned b2 = __shfl_xor_sync(0xffffffffu, bi, off);
-            if (better(v2, h2, t2, v, h, t) || (v2 == v && h2 == h && t2 == t && b2 < bi)) {
-                v = v2;
-                h = h2;
-                t = t2;
-                bi = b2;
-            }
-        }
-        if (lane == 0) {
-            const PeakSlot& ps = sl[bi];
-            const bool mirror = ps.h >= w.n_shift;
-            const unsigned sidx = mirror ? ps.h - w.n_shift : ps.h;
-            const float angle =
-                w.rule == kPeakPreAlign ? pre_peak_angle(ps.nb, ps.t, mirror) : peak_angle(ps.nb, ps.t, mirror);
-            const unsigned p = item / w.n_ref, q = item - p * w.n_ref;
-            const unsigned pg = w.p_first + p;
-            const float bx = w.base ? w.base[pg].x : 0.f, by = w.base ? w.base[pg].y : 0.f;
-            const float2 sf = w.shifts_f[sidx];
-            const size_t o = (size_t)q * w.p_total + pg;
-            w.d_out[o] = ps.v;
-            w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
-        }
-    };
+    float2* const gz = wsp + (size_t)g * kPairStride;
     PeakState st;
     st.reset(w.rule);
-    bool failed = false;
-    unsigned u = 0, n_done = 0;           // items finished (their bests parked)
-    bool pending = false;                 // an item parked and not merged yet
-    unsigned pending_item = 0;
-    for (; u < n_units; u++) {
-        const unsigned buf = u & 1u, item = unit_item(u), b = u % w.n_blocks;
+    unsigned n_done = 0;
+    for (unsigned u = 0; u < n_units; u++) {
+        const unsigned b = u % w.n_blocks;
         const unsigned s0 = b * w.block, nsb = min(w.block, w.n_shift - s0);
-        const bool ok = mbar_wait(full + buf, (u >> 1) & 1u, wlim);
-        float2* const zcur = buf ? zb1 : zb0;
-        // this group's shift columns into registers
-        float2 x[RR][16];
-#pragma unroll
-        for (int rr = 0; rr < RR; rr++) {
-            const unsigned sl = g + rr * groups;
-            if (ok && sl < nsb) {
-#pragma unroll
-                for (int m = 0; m < 16; m++)
-                    x[rr][m] = zcur[(l + 16 * m) * w.zw + sl];
-            }
+        if (!mbar_wait_abort(full, u & 1u, abort_flag, wlim)) {
+            *abort_flag = 1;
+            atomicExch(err, 1u);
+            return;
         }
-        // every column is in registers: the buffer now serves as the groups'
-        // FFT workspaces; the parks of the last finished item are visible
-        if (!__syncthreads_and(ok)) {
-            failed = true;
-            break;
-        }
-        if (pending && tid < 32)
-            merge(pending_item, slots + 64 * ((n_done - 1) & 1u));
-        pending = false;
-        float2* gz = zcur + g * kPairStride;
+        const bool has = (unsigned)g < nsb; // group-uniform
+        float2 x[16];
+        if (has) {
 #pragma unroll
-        for (int rr = 0; rr < RR; rr++) {
-            const unsigned sl = g + rr * groups;
-            if (sl < nsb) // group-uniform
-                fft_peak_regs<true>(x[rr], gz, tw + l * kTwRow, l, gmask, s0 + sl, w.n_shift, st, w.rule);
+            for (int m = 0; m < 16; m++)
+                x[m] = zb[(l + 16 * m) * w.zw + g];
         }
+        mbar_arrive(empty);
+        if (has)
+            fft_peak_regs<true>(x, gz, tw + l * kTwRow, l, gmask, s0 + g, w.n_shift, st, w.rule);
         if (b == w.n_blocks - 1) {
             // every shift of the pair has been searched: park the group's best
-            park_slot(slots + 64 * (n_done & 1u), st, g, l);
+            const unsigned set = n_done % kZfftRing;
+            if (!mbar_wait_abort(freed + set, ((n_done / kZfftRing) & 1u) ^ 1u, abort_flag, wlim)) {
+                *abort_flag = 1;
+                atomicExch(err, 1u);
+                return;
+            }
+            park_slot(slots + 64 * set, st, g, l);
+            mbar_arrive(parked + set);
             st.reset(w.rule);
-            pending = true;
-            pending_item = item;
             n_done++;
         }
-        __syncthreads(); // the buffer is free; the parks are visible
-        if (tid == 0 && u + 2 < n_units)
-            issue(u + 2);
-    }
-    if (!failed && pending && tid < 32)
-        merge(pending_item, slots + 64 * ((n_done - 1) & 1u));
-    if (failed && tid == 0) {
-        atomicExch(err, 1u);
-        // copies in flight land before the CTA ends (bounded)
-        for (unsigned v = u; v < std::min(u + 2, n_units) && !w.test_stall; v++)
-            mbar_wait(full + (v & 1u), (v >> 1) & 1u, wlim);
     }
 }
 
@@ -527,8 +570,8 @@ static size_t mma_smem(const SplitPlan& p) { return (size_t)p.n_stages * mma_sta
 
 static size_t fft_smem(const SplitPlan& p)
 {
-    const size_t zbuf = std::max((size_t)kRingLen * p.zw * sizeof(float2), (size_t)p.fft_groups * kPairStride * sizeof(float2));
-    return 2 * zbuf + 16 * kTwRow * sizeof(float2) + 128 * sizeof(PeakSlot) + 64;
+    return zfft_zbuf_bytes(p.zw) + (size_t)p.fft_groups * kPairStride * sizeof(float2) + 16 * kTwRow * sizeof(float2) +
+           kZfftRing * 64 * sizeof(PeakSlot) + (2 + 2 * kZfftRing) * sizeof(uint64_t) + 16;
 }
 
 bool split_plan(unsigned ring_num, unsigned n_shift, unsigned n_ref, SplitPlan& p)
@@ -656,9 +699,9 @@ cudaError_t launch_zfft_peak(const SplitPlan& p, const float2* z, unsigned n_par
     const size_t fs = fft_smem(p);
     const unsigned grid = std::min<unsigned>(n_part * n_ref, device_sms());
     cudaError_t e;
-    if ((e = opt_in_smem_k(zfft_peak_kernel<1>, fs)) != cudaSuccess)
+    if ((e = opt_in_smem_k(zfft_peak_kernel, fs)) != cudaSuccess)
         return e;
-    zfft_peak_kernel<1><<<grid, 16 * p.fft_groups, fs, stream>>>(fw, twiddle, err);
+    zfft_peak_kernel<<<grid, zfft_group_threads(p.fft_groups) + kZfftCtlThreads, fs, stream>>>(fw, twiddle, err);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

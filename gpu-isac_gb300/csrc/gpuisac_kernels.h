@@ -64,12 +64,44 @@ struct TexStack {
     cudaError_t build(const StackDesc& st, cudaStream_t stream);
     // build(), or -- when it fails (no memory for the copy, say) -- nothing:
     // returns the objects, or null after releasing any partial allocation;
-    // the caller then samples with the emulation, which computes the same taps
+    // the caller then samples with the emulation (the same texels and
+    // weights; the filtered value equal to the last bit or two)
     const unsigned long long* try_build(const StackDesc& st, cudaStream_t stream);
     const unsigned long long* objects() const { return d_objs; }
     void destroy_objects();
     void release();
 };
+
+// One stack's part of a TexSet fill: the destination layout and the rows
+// row_begin .. of the launch (tex_fill_jobs_kernel)
+struct TexFillJob {
+    const float* src;
+    unsigned char* mem;
+    size_t full_bytes, batch_bytes, pitch;
+    unsigned n, dim, batch, tex;
+    unsigned row_begin;
+};
+
+// Many stacks laid out as the reference's textures hold them (each as a
+// TexStack would), in one device region: prepare() lays them out (the region
+// only grows), creates the texture objects (objs, stack i's first at
+// obj_first[i]; the previous call's objects are destroyed) and the fill jobs
+// (jobs, rows).  The caller uploads the jobs and objects and fills with
+// launch_tex_fill_jobs, whose row count it reads from device memory.
+struct TexSet {
+    unsigned char* mem = nullptr;
+    size_t mem_bytes = 0;
+    std::vector<unsigned long long> objs;
+    std::vector<unsigned> obj_first;
+    std::vector<TexFillJob> jobs;
+    unsigned rows = 0;
+    cudaError_t prepare(const std::vector<StackDesc>& stacks);
+    void destroy_objects();
+    void release();
+};
+
+// hdr = {jobs, rows} in device memory; grid-stride over the rows, a warp per row
+cudaError_t launch_tex_fill_jobs(const TexFillJob* jobs, const unsigned* hdr, unsigned grid, cudaStream_t stream);
 
 // Whether the kernels sample through the texture unit (TexStack) where the
 // caller has one: on unless the environment sets GPUISAC_TEXTURE=0.
@@ -85,6 +117,47 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
                                  const float2* base, unsigned img0, unsigned n_img, int is_ref,
                                  float2* out, cudaStream_t stream, const unsigned* img_list = nullptr,
                                  const unsigned long long* tex_objs = nullptr);
+
+// A run of consecutive spectra rows of one stack: images img0 .. img0 +
+// n_img - 1 x n_shift shifts, written from `out` on ([n_img][n_shift] rows);
+// rows row_begin .. of the launch that holds the job.
+struct SpectraJob {
+    StackDesc st;
+    const unsigned long long* tex_objs; // texture objects of st, or null (the emulation)
+    const float2* base;                 // base shifts by image index in st, or null
+    const int2* shift_int;              // n_shift integer shifts
+    float2* out;
+    unsigned img0, n_img, n_shift;
+    int is_ref;
+    unsigned row_begin;
+};
+
+// The spectra of a job table: hdr = {first job, jobs, rows, lookup offset}
+// in device memory (jobs ordered by row_begin from 0); lut + hdr[3] holds,
+// per block of kJobLutRows rows, the index of the job holding the block's
+// first row.  One CTA per row: `grid` must cover the rows (CTAs past them
+// return); the same launch serves any table the device buffers hold.
+constexpr unsigned kJobLutRows = 32;
+cudaError_t launch_polar_spectra_jobs(const SpectraJob* jobs, const unsigned* hdr, const unsigned* lut,
+                                      const float2* tmpl, const float2* twiddle, unsigned ring_num, unsigned grid,
+                                      cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Rings of 512 samples (ring512.cu): spectra rows [ring][kSlots512] float2 in
+// the basis of the 256-sample rows (slot 0 = (F[0], F[256])), and the CCF /
+// inverse-FFT / peak search over them; tw512[e] = e^(-2 pi i e / 512).
+constexpr int kRingLen512 = 512;
+constexpr int kSlots512 = kRingLen512 / 2;
+cudaError_t launch_polar_spectra512(const StackDesc& st, const float2* tmpl, const float2* tw512, unsigned ring_num,
+                                    const int2* shift_int, unsigned n_shift, const float2* base, unsigned img0,
+                                    unsigned n_img, int is_ref, float2* out, cudaStream_t stream,
+                                    const unsigned long long* tex_objs);
+// results for particle i of sbj_sp to column p_first + i of d_out / peak_out
+// [n_ref][p_total]; base: base shifts by global particle index, or null
+cudaError_t launch_ccf_peak512(const float2* sbj_sp, const float2* ref_sp, const float2* tw512, unsigned ring_num,
+                               unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_first, unsigned p_total,
+                               const float2* shifts_f, const float2* base, float* d_out, float4* peak_out,
+                               cudaStream_t stream);
 
 // ---------------------------------------------------------------------------
 // Operands of the tensor-core contraction (ccf_split.cu).  For every spectrum
@@ -151,12 +224,16 @@ struct CcfGroup {
 enum { kPeakMref = 0, kPeakPreAlign = 1 };
 
 // Work of one CCF launch: either one group (groups == null, `one`) or a
-// device table of n_groups groups ordered by item_begin.
+// device table of n_groups groups ordered by item_begin.  With dyn set, the
+// table is groups + dyn[0] and its group and item counts are dyn[1], dyn[2]
+// in device memory (a recorded launch then serves any table of the buffer);
+// n_items is then only the host's bound for the grid.
 struct CcfWork {
     const CcfGroup* groups;
     CcfGroup one;
     unsigned n_groups;
     unsigned n_items;
+    const unsigned* dyn;
     unsigned ppc;     // particles per work item
     unsigned max_ref; // most references of any group (0: not known); 1 selects the one-reference contraction
     // failure-path tests only (gpuisac_test_stall_ccf): the kernels that stage

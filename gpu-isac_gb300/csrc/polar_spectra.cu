@@ -15,6 +15,7 @@
 // part) correlation at once.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -75,7 +76,7 @@ polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const f
                    unsigned ring_num, const int2* __restrict__ shift_int, unsigned n_shift,
                    const float2* __restrict__ base, unsigned img0, unsigned n_img, int is_ref,
                    float2* __restrict__ out, const unsigned* __restrict__ img_list,
-                   const unsigned long long* __restrict__ tex_objs, const OperandLayout& opnd)
+                   const unsigned long long* __restrict__ tex_objs, const OperandLayout& opnd, unsigned row)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // ring pair p's samples at polar[p * 2 * kPairStride + (r & 1) * 256 + angle];
@@ -85,7 +86,6 @@ polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const f
     float2* tw = reinterpret_cast<float2*>(polar + n_pairs * 2 * kPairStride);  // 256
     double* red = reinterpret_cast<double*>(tw + kRingLen);                   // 2 x 8 warps + 2
 
-    const unsigned row = blockIdx.x;
     const unsigned img_local = row / n_shift;
     const unsigned s = row - img_local * n_shift;
     if (img_local >= n_img)
@@ -262,7 +262,29 @@ polar_spectra_kernel(StackDesc st, const float2* __restrict__ tmpl, const float2
                      const unsigned long long* __restrict__ tex_objs)
 {
     polar_spectra_body<false>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base, img0, n_img, is_ref, out,
-                              img_list, tex_objs, OperandLayout());
+                              img_list, tex_objs, OperandLayout(), blockIdx.x);
+}
+
+// The same rows for a table of jobs (SpectraJobs), one CTA per row, the row
+// count read from device memory so that a recorded launch (grid = the
+// capacity) serves any table the buffers hold.  A row's job: the lookup entry
+// of its block of kJobLutRows rows (the job holding the block's first row),
+// then forward over the jobs that start inside the block.
+__global__ void __launch_bounds__(256, 5)
+polar_spectra_jobs_kernel(const SpectraJob* __restrict__ jobs, const unsigned* __restrict__ hdr,
+                          const unsigned* __restrict__ lut, const float2* __restrict__ tmpl,
+                          const float2* __restrict__ twiddle, unsigned ring_num)
+{
+    const unsigned row = blockIdx.x;
+    if (row >= hdr[2])
+        return;
+    const unsigned last = hdr[0] + hdr[1] - 1;
+    unsigned j = lut[hdr[3] + row / kJobLutRows];
+    while (j < last && jobs[j + 1].row_begin <= row)
+        j++;
+    const SpectraJob& jb = jobs[j];
+    polar_spectra_body<false>(jb.st, tmpl, twiddle, ring_num, jb.shift_int, jb.n_shift, jb.base, jb.img0, jb.n_img,
+                              jb.is_ref, jb.out, nullptr, jb.tex_objs, OperandLayout(), row - jb.row_begin);
 }
 
 __global__ void __launch_bounds__(256, 4)
@@ -272,7 +294,7 @@ polar_operands_kernel(StackDesc st, const float2* __restrict__ tmpl, const float
                       OperandLayout opnd, const unsigned long long* __restrict__ tex_objs)
 {
     polar_spectra_body<true>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base, img0, n_img, is_ref, nullptr,
-                             nullptr, tex_objs, opnd);
+                             nullptr, tex_objs, opnd, blockIdx.x);
 }
 
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
@@ -290,6 +312,21 @@ cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const 
     unsigned rows = n_img * n_shift;
     polar_spectra_kernel<<<rows, 256, smem, stream>>>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base,
                                                        img0, n_img, is_ref, out, img_list, tex_objs);
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_polar_spectra_jobs(const SpectraJob* jobs, const unsigned* hdr, const unsigned* lut,
+                                      const float2* tmpl, const float2* twiddle, unsigned ring_num, unsigned grid,
+                                      cudaStream_t stream)
+{
+    if (grid == 0)
+        return cudaSuccess;
+    cudaError_t e = opt_in_smem_k(polar_spectra_jobs_kernel, polar_spectra_smem_bytes(kMaxRingNum));
+    if (e != cudaSuccess)
+        return e;
+    polar_spectra_jobs_kernel<<<grid, 256, polar_spectra_smem_bytes(ring_num), stream>>>(jobs, hdr, lut, tmpl,
+                                                                                         twiddle, ring_num);
     g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
     return cudaGetLastError();
 }

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <vector>
 
 #include "gpuisac_kernels.h"
 
@@ -47,9 +48,188 @@ tex_fill_kernel(const float* __restrict__ src, unsigned n, unsigned dim, unsigne
         dst[x] = s[x];
 }
 
+// tex_fill_kernel over a table of stacks (TexFillJob, ordered by row_begin
+// from 0): one warp per destination row, persistent over hdr = {jobs, rows}
+__global__ void __launch_bounds__(256)
+tex_fill_jobs_kernel(const TexFillJob* __restrict__ jobs, const unsigned* __restrict__ hdr)
+{
+    const unsigned n_jobs = hdr[0], rows = hdr[1];
+    for (unsigned r = blockIdx.x * 8 + (threadIdx.x >> 5); r < rows; r += gridDim.x * 8) {
+        unsigned lo = 0, hi = n_jobs - 1;
+        while (lo < hi) {
+            const unsigned mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].row_begin <= r)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const TexFillJob& j = jobs[lo];
+        const unsigned dim = j.dim, per_batch = j.batch * dim;
+        const unsigned rl = r - j.row_begin;
+        const unsigned b = rl / per_batch, rb = rl - b * per_batch;
+        const unsigned t = rb / (j.tex * dim);
+        const unsigned in_seg = rb - t * j.tex * dim;
+        const unsigned jj = in_seg / dim, y = in_seg - jj * dim;
+        unsigned g = b * j.batch + t * j.tex + jj;
+        if (g >= j.n)
+            g -= j.batch;
+        float* dst = reinterpret_cast<float*>(j.mem + (size_t)b * j.batch_bytes + (size_t)t * j.full_bytes +
+                                              (size_t)in_seg * j.pitch);
+        const float* src = j.src + ((size_t)g * dim + y) * dim;
+        for (unsigned x = threadIdx.x & 31; x < dim; x += 32)
+            dst[x] = src[x];
+    }
+}
+
 size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// where a stack's textures live: row pitch, bytes of a full texture, of a
+// batch, of the whole layout; textures per batch, batches, images of a
+// batch's last texture
+struct TexGeometry {
+    size_t pitch, full_bytes, batch_bytes, need;
+    unsigned ntpb, nb, last_alloc;
+};
+
+cudaError_t tex_geometry(const StackDesc& st, int dev, TexGeometry& g)
+{
+    if (st.n == 0 || st.dim == 0 || st.batch == 0 || st.tex == 0 || st.batch > st.n)
+        return cudaErrorInvalidValue;
+    int tex_align = 512, pitch_align = 32;
+    cudaDeviceGetAttribute(&tex_align, cudaDevAttrTextureAlignment, dev);
+    cudaDeviceGetAttribute(&pitch_align, cudaDevAttrTexturePitchAlignment, dev);
+    const unsigned D = st.dim;
+    g.pitch = round_up((size_t)D * sizeof(float), (size_t)std::max(pitch_align, 4));
+    g.ntpb = (st.batch + st.tex - 1) / st.tex;
+    g.nb = (st.n + st.batch - 1) / st.batch;
+    g.last_alloc = st.batch - (g.ntpb - 1) * st.tex;
+    g.full_bytes = round_up((size_t)st.tex * D * g.pitch, (size_t)tex_align);
+    const size_t last_bytes = round_up((size_t)g.last_alloc * D * g.pitch, (size_t)tex_align);
+    g.batch_bytes = (size_t)(g.ntpb - 1) * g.full_bytes + last_bytes;
+    g.need = (size_t)g.nb * g.batch_bytes;
+    return cudaSuccess;
+}
+
+// one texture object per (batch, texture) segment of a layout at mem,
+// appended to objs
+cudaError_t create_tex_objects(unsigned char* mem, const StackDesc& st, const TexGeometry& g,
+                               std::vector<unsigned long long>& objs)
+{
+    for (unsigned b = 0; b < g.nb; b++)
+        for (unsigned t = 0; t < g.ntpb; t++) {
+            const unsigned alloc = (t != g.ntpb - 1) ? st.tex : g.last_alloc;
+            cudaResourceDesc rd{};
+            rd.resType = cudaResourceTypePitch2D;
+            rd.res.pitch2D.devPtr = mem + (size_t)b * g.batch_bytes + (size_t)t * g.full_bytes;
+            rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
+            rd.res.pitch2D.width = st.dim;
+            rd.res.pitch2D.height = (size_t)alloc * st.dim;
+            rd.res.pitch2D.pitchInBytes = g.pitch;
+            cudaTextureDesc td{};
+            td.addressMode[0] = cudaAddressModeClamp;
+            td.addressMode[1] = cudaAddressModeClamp;
+            td.filterMode = cudaFilterModeLinear;
+            td.readMode = cudaReadModeElementType;
+            td.normalizedCoords = 0;
+            cudaTextureObject_t o = 0;
+            const cudaError_t e = cudaCreateTextureObject(&o, &rd, &td, nullptr);
+            if (e != cudaSuccess)
+                return e;
+            objs.push_back((unsigned long long)o);
+        }
+    return cudaSuccess;
+}
+
 } // namespace
+
+void TexSet::destroy_objects()
+{
+    for (unsigned long long o : objs)
+        cudaDestroyTextureObject((cudaTextureObject_t)o);
+    objs.clear();
+}
+
+void TexSet::release()
+{
+    destroy_objects();
+    if (mem)
+        cudaFree(mem);
+    mem = nullptr;
+    mem_bytes = 0;
+    jobs.clear();
+    obj_first.clear();
+    rows = 0;
+}
+
+cudaError_t TexSet::prepare(const std::vector<StackDesc>& stacks)
+{
+    destroy_objects();
+    jobs.clear();
+    obj_first.clear();
+    rows = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    std::vector<TexGeometry> geo(stacks.size());
+    std::vector<size_t> off(stacks.size());
+    size_t need = 0, total_rows = 0;
+    for (size_t i = 0; i < stacks.size(); i++) {
+        e = tex_geometry(stacks[i], dev, geo[i]);
+        if (e != cudaSuccess)
+            return e;
+        off[i] = need;
+        need += geo[i].need; // every part of a layout is a multiple of the texture alignment
+        total_rows += (size_t)geo[i].nb * stacks[i].batch * stacks[i].dim;
+    }
+    if (total_rows > 0x7FFFFFFFull)
+        return cudaErrorInvalidValue;
+    if (need > mem_bytes) {
+        if (mem)
+            cudaFree(mem);
+        mem = nullptr;
+        mem_bytes = 0;
+        e = cudaMalloc(&mem, need);
+        if (e != cudaSuccess)
+            return e;
+        mem_bytes = need;
+    }
+    size_t row = 0;
+    for (size_t i = 0; i < stacks.size(); i++) {
+        const StackDesc& st = stacks[i];
+        const TexGeometry& g = geo[i];
+        obj_first.push_back((unsigned)objs.size());
+        e = create_tex_objects(mem + off[i], st, g, objs);
+        if (e != cudaSuccess) {
+            destroy_objects();
+            return e;
+        }
+        TexFillJob j{};
+        j.src = st.img;
+        j.mem = mem + off[i];
+        j.full_bytes = g.full_bytes;
+        j.batch_bytes = g.batch_bytes;
+        j.pitch = g.pitch;
+        j.n = st.n;
+        j.dim = st.dim;
+        j.batch = st.batch;
+        j.tex = st.tex;
+        j.row_begin = (unsigned)row;
+        jobs.push_back(j);
+        row += (size_t)g.nb * st.batch * st.dim;
+    }
+    rows = (unsigned)row;
+    return cudaSuccess;
+}
+
+cudaError_t launch_tex_fill_jobs(const TexFillJob* jobs, const unsigned* hdr, unsigned grid, cudaStream_t stream)
+{
+    if (grid == 0)
+        return cudaSuccess;
+    tex_fill_jobs_kernel<<<grid, 256, 0, stream>>>(jobs, hdr);
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
 
 bool texture_unit_enabled()
 {
@@ -95,89 +275,57 @@ cudaError_t TexStack::build(const StackDesc& st, cudaStream_t stream)
 
 cudaError_t TexStack::prepare(const StackDesc& st)
 {
-    if (st.n == 0 || st.dim == 0 || st.batch == 0 || st.tex == 0 || st.batch > st.n)
-        return cudaErrorInvalidValue;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return e;
-    int tex_align = 512, pitch_align = 32;
-    cudaDeviceGetAttribute(&tex_align, cudaDevAttrTextureAlignment, dev);
-    cudaDeviceGetAttribute(&pitch_align, cudaDevAttrTexturePitchAlignment, dev);
-    const unsigned D = st.dim;
-    const size_t pitch = round_up((size_t)D * sizeof(float), (size_t)std::max(pitch_align, 4));
-    const unsigned ntpb = (st.batch + st.tex - 1) / st.tex;     // textures per batch
-    const unsigned nb = (st.n + st.batch - 1) / st.batch;        // batches
-    const unsigned last_alloc = st.batch - (ntpb - 1) * st.tex;  // images of a batch's last texture
-    const size_t full_bytes = round_up((size_t)st.tex * D * pitch, (size_t)tex_align);
-    const size_t last_bytes = round_up((size_t)last_alloc * D * pitch, (size_t)tex_align);
-    const size_t batch_bytes = (size_t)(ntpb - 1) * full_bytes + last_bytes;
-    const size_t need = (size_t)nb * batch_bytes;
-
-    const bool same_layout = mem && need <= mem_bytes && dim == D && batch == st.batch && tex == st.tex &&
-                             n == st.n && pitch_ == pitch && device == dev;
-    if (!same_layout) {
-        destroy_objects();
-        if (need > mem_bytes) {
-            if (mem)
-                cudaFree(mem);
-            mem = nullptr;
-            mem_bytes = 0;
-            e = cudaMalloc(&mem, need);
-            if (e != cudaSuccess)
-                return e;
-            mem_bytes = need;
-        }
-        const unsigned n_seg = nb * ntpb;
-        objs.resize(n_seg);
-        for (unsigned b = 0; b < nb; b++)
-            for (unsigned t = 0; t < ntpb; t++) {
-                const unsigned alloc = (t != ntpb - 1) ? st.tex : last_alloc;
-                cudaResourceDesc rd{};
-                rd.resType = cudaResourceTypePitch2D;
-                rd.res.pitch2D.devPtr = mem + (size_t)b * batch_bytes + (size_t)t * full_bytes;
-                rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
-                rd.res.pitch2D.width = D;
-                rd.res.pitch2D.height = (size_t)alloc * D;
-                rd.res.pitch2D.pitchInBytes = pitch;
-                cudaTextureDesc td{};
-                td.addressMode[0] = cudaAddressModeClamp;
-                td.addressMode[1] = cudaAddressModeClamp;
-                td.filterMode = cudaFilterModeLinear;
-                td.readMode = cudaReadModeElementType;
-                td.normalizedCoords = 0;
-                cudaTextureObject_t o = 0;
-                e = cudaCreateTextureObject(&o, &rd, &td, nullptr);
-                if (e != cudaSuccess) {
-                    objs.resize(b * ntpb + t);
-                    destroy_objects();
-                    return e;
-                }
-                objs[b * ntpb + t] = (unsigned long long)o;
-            }
-        if (d_objs_n < n_seg) {
-            if (d_objs)
-                cudaFree(d_objs);
-            d_objs = nullptr;
-            d_objs_n = 0;
-            e = cudaMalloc(&d_objs, n_seg * sizeof(unsigned long long));
-            if (e != cudaSuccess)
-                return e;
-            d_objs_n = n_seg;
-        }
-        e = cudaMemcpy(d_objs, objs.data(), n_seg * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+    TexGeometry g;
+    e = tex_geometry(st, dev, g);
+    if (e != cudaSuccess)
+        return e;
+    const bool same_layout = mem && g.need <= mem_bytes && dim == st.dim && batch == st.batch && tex == st.tex &&
+                             n == st.n && pitch_ == g.pitch && device == dev;
+    if (same_layout)
+        return cudaSuccess;
+    destroy_objects();
+    if (g.need > mem_bytes) {
+        if (mem)
+            cudaFree(mem);
+        mem = nullptr;
+        mem_bytes = 0;
+        e = cudaMalloc(&mem, g.need);
         if (e != cudaSuccess)
             return e;
-        n = st.n;
-        dim = D;
-        batch = st.batch;
-        tex = st.tex;
-        pitch_ = pitch;
-        full_bytes_ = full_bytes;
-        batch_bytes_ = batch_bytes;
-        n_batches = nb;
-        device = dev;
+        mem_bytes = g.need;
     }
+    e = create_tex_objects(mem, st, g, objs);
+    if (e != cudaSuccess) {
+        destroy_objects();
+        return e;
+    }
+    const size_t n_seg = objs.size();
+    if (d_objs_n < n_seg) {
+        if (d_objs)
+            cudaFree(d_objs);
+        d_objs = nullptr;
+        d_objs_n = 0;
+        e = cudaMalloc(&d_objs, n_seg * sizeof(unsigned long long));
+        if (e != cudaSuccess)
+            return e;
+        d_objs_n = n_seg;
+    }
+    e = cudaMemcpy(d_objs, objs.data(), n_seg * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        return e;
+    n = st.n;
+    dim = st.dim;
+    batch = st.batch;
+    tex = st.tex;
+    pitch_ = g.pitch;
+    full_bytes_ = g.full_bytes;
+    batch_bytes_ = g.batch_bytes;
+    n_batches = g.nb;
+    device = dev;
     return cudaSuccess;
 }
 

@@ -49,8 +49,14 @@ EXPORTS = (
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
     "gpuisac_ref_free_averages", "gpuisac_set_contraction", "gpuisac_get_contraction", "gpuisac_test_stall_ccf", "gpuisac_normalize_mask",
-    "gpuisac_split_plan",
+    "gpuisac_split_plan", "gpuisac_groups_stats",
 )
+
+
+class GpuisacGroupStats(ctypes.Structure):
+    """Mirror of GpuisacGroupStats (include/gpu_aln_pack.h)."""
+    _fields_ = [("plan_ms", ctypes.c_double), ("record_ms", ctypes.c_double), ("waves", ctypes.c_uint),
+                ("graph_launches", ctypes.c_uint), ("graphs_recorded", ctypes.c_uint)]
 
 
 class GpuisacGroup(ctypes.Structure):
@@ -128,6 +134,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     L.gpuisac_multi_ref_align_groups_device.restype = ctypes.c_int
+    L.gpuisac_groups_stats.argtypes = [ctypes.POINTER(GpuisacGroupStats)]
+    L.gpuisac_groups_stats.restype = ctypes.c_int
     vp, ci, cl, cf, cu = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_float, ctypes.c_uint
     L.gpuisac_align_proposals_device.argtypes = [aln_cfg_ptr, vp, vp, vp, vp, cu, vp, cu, vp, vp, vp]
     L.gpuisac_nn_features.argtypes = [vp, cu, cu, cu, vp, vp, vp, vp]

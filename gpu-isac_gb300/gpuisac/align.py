@@ -119,16 +119,17 @@ def _multi_ref_align(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_
 
 def multi_ref_align_device(particles, refs, ring_num: int, shift_rng_x: float, shift_rng_y: float,
                            shift_step: float = 1.0, base_shifts=None, stream=None, d_out=None, peak_out=None,
-                           contraction_mode: str | None = None):
+                           contraction_mode: str | None = None, ring_len: int = 256):
     """Device-resident form on torch CUDA tensors: returns (d [R][P], peak [R][P][4]).
-    contraction_mode: "fp32" or "bf16x3" for this call (None: the current mode)."""
+    contraction_mode: "fp32" or "bf16x3" for this call (None: the current mode);
+    ring_len: 256 or 512 samples per ring (512 computes in FP32 whatever the mode)."""
     with contraction(contraction_mode):
         return _multi_ref_align_device(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_step,
-                                       base_shifts, stream, d_out, peak_out)
+                                       base_shifts, stream, d_out, peak_out, ring_len)
 
 
 def _multi_ref_align_device(particles, refs, ring_num, shift_rng_x, shift_rng_y, shift_step, base_shifts, stream,
-                            d_out, peak_out):
+                            d_out, peak_out, ring_len=256):
     import torch
 
     if not (particles.is_cuda and refs.is_cuda):
@@ -137,7 +138,7 @@ def _multi_ref_align_device(particles, refs, ring_num, shift_rng_x, shift_rng_y,
     refs = refs.contiguous().float()
     P, D = particles.shape[0], particles.shape[1]
     R = refs.shape[0]
-    cfg = make_config(P, R, D, ring_num, 256, shift_step, shift_rng_x, shift_rng_y)
+    cfg = make_config(P, R, D, ring_num, ring_len, shift_step, shift_rng_x, shift_rng_y)
     if d_out is None:
         d_out = torch.empty((R, P), dtype=torch.float32, device=particles.device)
     if peak_out is None:
@@ -226,6 +227,19 @@ def multi_ref_align_groups_device(particles, refs, groups, ring_num: int, shift_
         _lib.check(L)
         raise GpuIsacError(f"gpuisac_multi_ref_align_groups_device failed ({rc})")
     return d, pk, offsets
+
+
+def groups_stats() -> dict:
+    """What the last multi_ref_align_groups_device call did
+    (gpuisac_groups_stats): host plan time, graph recording time (0 when a
+    recorded graph was replayed), waves, launches in the graph."""
+    from ._lib import GpuisacGroupStats
+    L = _lib.load()
+    s = GpuisacGroupStats()
+    if L.gpuisac_groups_stats(ctypes.byref(s)):
+        _lib.check(L)
+    return {"plan_ms": s.plan_ms, "record_ms": s.record_ms, "waves": s.waves,
+            "graph_launches": s.graph_launches, "graph_recorded": bool(s.graphs_recorded)}
 
 
 def align_proposals_device(particles, refs, proposals, ring_num: int, shift_rng_x: float, shift_rng_y: float,

@@ -57,9 +57,9 @@ def ormq(images, refs, xrng, yrng, step, mode, numr, cnx, cny, delta: float = 0.
     if float(delta) != 0.0:
         raise ValueError("delta != 0 (restricted angular search) is not on this path")
     ring_num, ring_len = numr_rings(numr)
-    if ring_len != 256:
+    if ring_len not in (256, 512):
         raise ValueError(f"the last ring's length is {ring_len}; this path samples every ring at 256 "
-                         "(the reference GPU path's ring length)")
+                         "(the reference GPU path's ring length) or 512")
     sx_r, sy_r = _shift_range(xrng, step), _shift_range(yrng, step)
     device = hasattr(images, "is_cuda") and images.is_cuda
     single = refs.ndim == 2
@@ -73,12 +73,12 @@ def ormq(images, refs, xrng, yrng, step, mode, numr, cnx, cny, delta: float = 0.
         import torch
         base = torch.tensor([bx, by], dtype=torch.float32, device=images.device).repeat(P, 1)
         d, pk = multi_ref_align_device(images, refs, ring_num, sx_r, sy_r, float(step), base_shifts=base,
-                                       contraction_mode=contraction_mode)
+                                       contraction_mode=contraction_mode, ring_len=ring_len)
         d, pk = d.cpu().numpy(), pk.cpu().numpy()
     else:
         base = np.tile(np.array([bx, by], np.float32), (P, 1))
         pl, d = multi_ref_align(np.asarray(images, np.float32), np.asarray(refs, np.float32), ring_num, sx_r, sy_r,
-                                float(step), base_shifts=base, contraction_mode=contraction_mode)
+                                float(step), base_shifts=base, contraction_mode=contraction_mode, ring_len=ring_len)
         pk = pl.reshape(refs.shape[0], P, 4)
     pk = pk.astype(np.float64)
     ang = pk[..., 0]

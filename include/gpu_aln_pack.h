@@ -229,14 +229,30 @@ typedef struct GpuisacGroup {
  * each group's particles against its own references -- in one pass over
  * device stacks: cfg gives the shared geometry (img_dim, ring_num, ring_len,
  * shift grid) and, in sbj_num / ref_num, the stack sizes.  Each group's
- * results equal those of a separate alignment of that group.  The launch
- * sequence is recorded in a CUDA graph and replayed when the identical call
- * (same groups, pointers, stream) is made again.  Blocks until done.
+ * results equal those of a separate alignment of that group.  The launches
+ * (one texture fill, then a spectra and a CCF launch per wave of particles)
+ * read their work from device tables; the sequence is recorded in a CUDA
+ * graph once per number of waves and tile shape and replayed by every later
+ * call of that shape, whatever its groups.  Blocks until done.
  * Returns 0 or an error code. */
 int gpuisac_multi_ref_align_groups_device(const AlignConfig *cfg, const GpuisacGroup *groups,
                                           unsigned int n_groups, const float *sbj, const float *ref,
                                           const float *base_shift, float *d_out, float *peak_out,
                                           void *stream);
+
+/* What the last gpuisac_multi_ref_align_groups_device call of the process
+ * did: host milliseconds from entry to its tables and texture objects being
+ * uploaded (plan_ms), milliseconds recording and instantiating a new launch
+ * graph (record_ms; 0 when a recorded one was replayed), waves of particles,
+ * kernel launches in the graph, and whether a graph was recorded. */
+typedef struct GpuisacGroupStats {
+    double plan_ms;
+    double record_ms;
+    unsigned int waves;
+    unsigned int graph_launches;
+    unsigned int graphs_recorded;
+} GpuisacGroupStats;
+int gpuisac_groups_stats(GpuisacGroupStats *out);
 
 /* No counterpart in the reference.  The exhaustive shift x angle x mirror
  * search of selected particles against k references each: particle

@@ -37,10 +37,10 @@ def cs_bound(ring_num, ring_len=256):
 NEAR_ZERO = 0.01
 
 
-def compare(peak_g, d_g, peak_o, d_o, ring_num=None):
+def compare(peak_g, d_g, peak_o, d_o, ring_num=None, ring_len=256):
     """peak_* [R][P][4], d_* [R][P]; with ring_num, peak values are compared
     relative to max(|d|, NEAR_ZERO x the Cauchy-Schwarz bound)"""
-    floor = NEAR_ZERO * cs_bound(ring_num) if ring_num else 1e-30
+    floor = NEAR_ZERO * cs_bound(ring_num, ring_len) if ring_num else 1e-30
     rel = np.abs(d_g.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), floor)
     assert rel.max() <= PEAK_RTOL, rel.max()
     same_tuple = (peak_g[..., 1:] == peak_o[..., 1:]).all(-1) & (circ_diff(peak_g[..., 0], peak_o[..., 0]) < ANGLE_TOL)

@@ -7,7 +7,10 @@ FP64 oracle on the same seeded inputs (gpuisac.synth):
                      generator against all 200 references, rings 1..35,
                      shifts +-3 (49), SNR 0.05;
   config 4 slice     200 x 128^2 particles against 100 of the 500
-                     references, rings 1..61, shifts +-4 (81), SNR 0.03.
+                     references, rings 1..61, shifts +-4 (81), SNR 0.03;
+                     once at 256 samples per ring (the reference GPU
+                     driver's ring length) and once at 512 (Numrinit's
+                     maximum ring length for a last ring of 61).
 
 Bars (floating point): every peak value within 1e-4 relative of the FP64
 oracle -- relative to max(|d|, 1% of the Cauchy-Schwarz bound L^2 sum(r+1)
@@ -33,6 +36,7 @@ CONFIGS = {
     "config0_full": dict(P=2000, D=64, R=16, NR=29, rng=2, snr=0.1, radius=28.0, seed_idx=0),
     "config1_slice": dict(P=1000, D=76, R=200, NR=35, rng=3, snr=0.05, radius=34.0, seed_idx=1),
     "config4_slice": dict(P=200, D=128, R=100, NR=61, rng=4, snr=0.03, radius=60.0, seed_idx=4),
+    "config4_slice_l512": dict(P=200, D=128, R=100, NR=61, rng=4, snr=0.03, radius=60.0, seed_idx=4, L=512),
 }
 
 _cache = {}
@@ -45,7 +49,8 @@ def case(name, oracle_mod, tex):
         c = CONFIGS[name]
         st = synth.make_stack(c["P"], c["D"], c["R"], c["rng"], c["snr"], c["radius"],
                               synth.SEED_BASE + c["seed_idx"])
-        cfg = oracle.make_cfg(c["P"], c["R"], c["D"], c["NR"], 256, 1.0, float(c["rng"]), float(c["rng"]))
+        cfg = oracle.make_cfg(c["P"], c["R"], c["D"], c["NR"], c.get("L", 256), 1.0, float(c["rng"]),
+                              float(c["rng"]))
         lay = oracle.reference_layout(cfg)
         lay = oracle.OrcLayout(lay.sbj_batch, tex, lay.ref_batch)
         peak_o, d_o = oracle_mod.multi_ref_align(cfg, lay, st.particles, st.refs, precision="f64")
@@ -58,11 +63,14 @@ def case(name, oracle_mod, tex):
 def test_config_parity_vs_fp64_oracle(gpulib, cuda, oracle_mod, name, mode):
     from gpuisac import multi_ref_align
     c = CONFIGS[name]
+    L = c.get("L", 256)
+    if L == 512 and mode == "bf16x3":
+        pytest.skip("512-sample rings contract in FP32 in either mode")
     st, peak_o, d_o = case(name, oracle_mod, gpulib.get_texture_limit(c["D"]))
-    pl, d = multi_ref_align(st.particles, st.refs, c["NR"], float(c["rng"]), float(c["rng"]),
+    pl, d = multi_ref_align(st.particles, st.refs, c["NR"], float(c["rng"]), float(c["rng"]), ring_len=L,
                             contraction_mode=mode)
-    rel, best, pairs = compare(pl.reshape(c["R"], c["P"], 4), d, peak_o, d_o, ring_num=c["NR"])
-    near = (np.abs(d_o) < NEAR_ZERO * cs_bound(c["NR"])).sum()
+    rel, best, pairs = compare(pl.reshape(c["R"], c["P"], 4), d, peak_o, d_o, ring_num=c["NR"], ring_len=L)
+    near = (np.abs(d_o) < NEAR_ZERO * cs_bound(c["NR"], L)).sum()
     strict = np.abs(d.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), 1e-30)
     print(f"{name} {mode}: max rel peak err {rel:.2e} ({near} near-zero peaks; plain relative {strict.max():.2e}), "
           f"same best {best:.4f}, same tuples {pairs:.4f}")

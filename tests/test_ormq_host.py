@@ -30,7 +30,8 @@ def test_numr_rings_of_the_workload_layouts():
     from gpuisac.ormq import numr_rings
     assert numr_rings(numrinit(1, 29)) == (29, 256)
     assert numr_rings(numrinit(1, 35)) == (35, 256)
-    assert numr_rings(numrinit(1, 61)) == (61, 512)  # the large-box layout: 512, refused below
+    assert numr_rings(numrinit(1, 61)) == (61, 512)  # the large-box layout
+    assert numr_rings(numrinit(1, 90)) == (90, 1024)  # refused below
     with pytest.raises(ValueError):
         numr_rings(numrinit(2, 30))                  # rings must start at 1
     with pytest.raises(ValueError):
@@ -38,7 +39,7 @@ def test_numr_rings_of_the_workload_layouts():
 
 
 @pytest.mark.parametrize("kw,msg", [(dict(mode="H"), "full-circle"), (dict(delta=1.0), "delta"),
-                                    (dict(numr=numrinit(1, 61)), "256"), (dict(xrng=[1.0, 2.0]), "symmetric")])
+                                    (dict(numr=numrinit(1, 90)), "256"), (dict(xrng=[1.0, 2.0]), "symmetric")])
 def test_ormq_refuses_what_the_gpu_path_does_not_compute(kw, msg):
     from gpuisac.ormq import ormq
     args = dict(images=np.zeros((2, 64, 64), np.float32), refs=np.zeros((64, 64), np.float32), xrng=[2.0, 2.0],
