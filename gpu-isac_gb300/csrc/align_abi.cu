@@ -1039,6 +1039,31 @@ int gpuisac_ccf_peak_device(const AlignConfig* cfg, const float* sbj_spectra, co
 
 unsigned long long gpuisac_launch_count(void) { return g_kernel_launches.load(); }
 
+int gpuisac_checked_failures(unsigned long long* first)
+{
+#ifdef GPUISAC_CHECKED
+    void (*readers[])(unsigned&, unsigned long long&) = {checked_read_spectra, checked_read_split, checked_read_ccf,
+                                                         checked_read_ring512};
+    unsigned total = 0;
+    unsigned long long f = 0;
+    for (auto rd : readers) {
+        unsigned c = 0;
+        unsigned long long fi = 0;
+        rd(c, fi);
+        if (c && !total)
+            f = fi;
+        total += c;
+    }
+    if (first)
+        *first = f;
+    return (int)total;
+#else
+    if (first)
+        *first = 0;
+    return -1;
+#endif
+}
+
 int gpuisac_set_contraction(int mode)
 {
     if (mode != GPUISAC_CONTRACTION_FP32 && mode != GPUISAC_CONTRACTION_BF16X3) {

@@ -256,8 +256,10 @@ __device__ __forceinline__ void merge_slots(PeakSlot* slots, int tid, int qt, in
         const float by = base ? base[pg].y : 0.f;
         const float2 sf = shifts_f[sidx];
         const size_t o = (size_t)(q0 + tid) * p_total + pg;
-        d_out[o] = ps.v;
-        peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+        if (GPUISAC_IN_BOUNDS(kChkMergeOut, o, (size_t)n_ref * p_total)) {
+            d_out[o] = ps.v;
+            peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+        }
     }
     phase_sync<BAR, N>();
 }

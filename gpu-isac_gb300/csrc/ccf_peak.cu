@@ -131,18 +131,22 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
 
     const uint32_t wlim = wait_tries(w.wait_iters);
     // copies of shift group s0 of particle p of group g (called by thread 0)
-    auto issue = [&](const float2* sp, unsigned p, unsigned s0) {
+    auto issue = [&](const CcfGroup& gg, unsigned p, unsigned s0) {
+        const float2* sp = gg.sbj_sp;
         if (w.test_stall)
             return;
         unsigned nv = min((unsigned)NSI, n_shift - s0);
         fence_proxy_async();
         mbar_expect_tx(bar, nv * row_bytes);
-        for (unsigned i = 0; i < nv; i++)
-            bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sp + ((size_t)p * n_shift + s0 + i) * ring_num * kSlots,
-                     row_bytes, bar);
+        for (unsigned i = 0; i < nv; i++) {
+            const size_t at = ((size_t)p * n_shift + s0 + i) * ring_num * kSlots;
+            if (GPUISAC_IN_BOUNDS(kChkCcfRow, at + (size_t)ring_num * kSlots - 1,
+                                  (size_t)gg.n_part * n_shift * ring_num * kSlots))
+                bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sp + at, row_bytes, bar);
+        }
     };
     if (tid == 0)
-        issue(grp.sbj_sp, pb, 0);
+        issue(grp, pb, 0);
     uint32_t phase = 0;
     bool failed = false;
 
@@ -249,11 +253,11 @@ ccf_peak_tmem_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned rin
                 // next copies overlap the FFT phase
                 if (tid == 0) {
                     if (s0 + NSI < n_shift)
-                        issue(grp.sbj_sp, p, s0 + NSI);
+                        issue(grp, p, s0 + NSI);
                     else if (p + 1 < pe)
-                        issue(grp.sbj_sp, p + 1, 0);
+                        issue(grp, p + 1, 0);
                     else if (has_next)
-                        issue(ngrp.sbj_sp, npb, 0);
+                        issue(ngrp, npb, 0);
                 }
 #pragma unroll
                 for (int ii = 0; ii < 2; ii++)
@@ -382,7 +386,8 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
         // particles start at p0 and number np
         const uint32_t wlim = wait_tries(w.wait_iters);
         // returns whether copies were issued
-        auto issue = [&](const float2* sp, unsigned p0, unsigned np, unsigned v0) -> bool {
+        auto issue = [&](const CcfGroup& gg, unsigned p0, unsigned np, unsigned v0) -> bool {
+            const float2* sp = gg.sbj_sp;
             if (w.test_stall)
                 return false;
             unsigned nv = 0;
@@ -394,15 +399,17 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             mbar_expect_tx(bar, nv * row_bytes);
             for (unsigned i = 0; i < (unsigned)NSI; i++) {
                 const unsigned v = v0 + i, pl = v / vstride, sv = v - pl * vstride;
-                if (pl < np && sv < n_shift)
-                    bulk_g2s(sbuf + (size_t)i * nrp * kSlots,
-                             sp + ((size_t)(p0 + pl) * n_shift + sv) * ring_num * kSlots, row_bytes, bar);
+                const size_t at = ((size_t)(p0 + pl) * n_shift + sv) * ring_num * kSlots;
+                if (pl < np && sv < n_shift &&
+                    GPUISAC_IN_BOUNDS(kChkCcfRow, at + (size_t)ring_num * kSlots - 1,
+                                      (size_t)gg.n_part * n_shift * ring_num * kSlots))
+                    bulk_g2s(sbuf + (size_t)i * nrp * kSlots, sp + at, row_bytes, bar);
             }
             return true;
         };
         bool pending = false; // thread 0: copies in flight
         if (tid == 0)
-            pending = issue(grp.sbj_sp, pb, pe - pb, 0);
+            pending = issue(grp, pb, pe - pb, 0);
         unsigned it = 0;
         while (!failed) {
             // this item's references -> tensor memory (both halves read every ring)
@@ -513,9 +520,9 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     tmem_fence_after();
                     if (tid == 0) {
                         if (v0 + NSI < nrows)
-                            pending = issue(grp.sbj_sp, pb, pe - pb, v0 + NSI);
+                            pending = issue(grp, pb, pe - pb, v0 + NSI);
                         else if (has_next)
-                            pending = issue(ngrp.sbj_sp, npb, npe - npb, 0);
+                            pending = issue(ngrp, npb, npe - npb, 0);
                     }
                     // ---- hand the pair spectra to the FFT side ----
                     float2* zb = zbuf + (size_t)b * NP * kPairStride;
@@ -882,6 +889,8 @@ static unsigned persistent_grid(unsigned n_items, unsigned ctas_per_sm)
 namespace {
 std::atomic<unsigned> g_test_stall{0}, g_test_wait_iters{0};
 } // namespace
+
+GPUISAC_CHECKED_READER(checked_read_ccf)
 
 void ccf_test_settings(unsigned& stall, unsigned& wait_iters)
 {

@@ -16,14 +16,16 @@
 // kernels, each launched once per particle chunk:
 //
 // ccf_mma_kernel    persistent; work item = (particle, shift block, reference
-//                   tile); 192 threads: warp 0 issues the bulk copies of each
+//                   tile); 576 threads: warp 0 issues the bulk copies of each
 //                   slot's operands into a ring of shared-memory stages, one
 //                   thread of warp 1 issues the 3 x K/16 tcgen05.mma of a slot
 //                   (M = 128 lanes = 64 shifts x {a, b}, N = 2 x references)
-//                   into one of two accumulators in tensor memory, and warps
-//                   2-5 drain the other accumulator with tcgen05.ld, pair the
-//                   a/b lanes by shuffle and write Z[k], Z[256-k] of every
-//                   (shift, reference) pair.
+//                   into one of two accumulators in tensor memory, and 16
+//                   drain warps (four per lane quadrant) drain the other
+//                   accumulator with tcgen05.ld and store every row's ring
+//                   sums (sum u, sum v) per reference, the a and b rows of a
+//                   shift side by side; the FFT kernel assembles Z[k] and
+//                   Z[256-k] of each (shift, reference) pair from them.
 // zfft_peak_kernel  persistent; work item = (particle, reference); the Z block
 //                   of each shift block is bulk-copied into a shared buffer
 //                   as soon as every 16-thread group has taken its shift's
@@ -183,10 +185,18 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
                     mbar_expect_tx(full + st, 2u * (a_copy + b_copy));
                     const unsigned char* as = a_src + (size_t)k * w.sop_slot;
                     const unsigned char* bs = b_src + (size_t)k * w.rop_slot;
-                    bulk_g2s(sb, as, a_copy, full + st);
-                    bulk_g2s(sb + a_bytes, as + a_copy, a_copy, full + st);
-                    bulk_g2s(sb + 2 * a_bytes, bs, b_copy, full + st);
-                    bulk_g2s(sb + 2 * a_bytes + b_bytes, bs + b_copy, b_copy, full + st);
+                    // (checked build: an out-of-range copy is left out and the
+                    // stage's bounded wait reports the call as failed)
+                    const bool a_in = GPUISAC_IN_BOUNDS(kChkMmaA, (size_t)(as - w.sop) + 2 * a_copy - 1,
+                                                        (size_t)w.n_part * w.n_blocks * kSlots * w.sop_slot);
+                    const bool b_in = GPUISAC_IN_BOUNDS(kChkMmaB, (size_t)(bs - w.rop) + 2 * b_copy - 1,
+                                                        (size_t)w.n_rtiles * kSlots * w.rop_slot);
+                    if (a_in && b_in) {
+                        bulk_g2s(sb, as, a_copy, full + st);
+                        bulk_g2s(sb + a_bytes, as + a_copy, a_copy, full + st);
+                        bulk_g2s(sb + 2 * a_bytes, bs, b_copy, full + st);
+                        bulk_g2s(sb + 2 * a_bytes + b_bytes, bs + b_copy, b_copy, full + st);
+                    }
                 }
             }
             if (failed) {
@@ -253,7 +263,6 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
         const unsigned part = (unsigned)(warp - 2) >> 2; // which chunks: part, part + kDrainPerQuad, ...
         const unsigned row = 32 * quad + lane;      // operand row = 2 shift + {0: a, 1: b}
         const unsigned sl = row >> 1;               // shift within the block
-        const bool is_b = row & 1u;
         uint32_t it = 0;
         for (unsigned item = blockIdx.x; item < w.n_items && !failed; item += gridDim.x) {
             const unsigned t = item % w.n_rtiles, pb = item / w.n_rtiles;
@@ -261,8 +270,11 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
             const unsigned q0 = t * w.rblock, nq = min(w.rblock, w.n_ref - q0);
             const unsigned s0 = b * w.block, nsb = min(w.block, w.n_shift - s0);
             const bool row_ok = sl < nsb;
-            // Z of (p, q, b): [256][zw] float2, shift fastest
-            float2* zbase = w.z + ((size_t)(p * w.n_ref + q0) * w.n_blocks + b) * kRingLen * w.zw + sl;
+            // ring sums of (p, q, b): [128 slots][zw shifts][a, b] float2, each
+            // entry a row's (sum u, sum v); the 32 rows of a warp store 256
+            // contiguous bytes per reference, and the FFT kernel assembles
+            // Z[k] = (sum u a, sum u b) and Z[256-k] = (sum v b, sum v a)
+            float2* zbase = w.z + ((size_t)(p * w.n_ref + q0) * w.n_blocks + b) * kRingLen * w.zw + row;
             const size_t zq = (size_t)w.n_blocks * kRingLen * w.zw; // between references
             const unsigned nchunk = (2 * nq + 15) / 16;
             const unsigned nj = nchunk > part ? (nchunk - part + kDrainPerQuad - 1) / kDrainPerQuad : 0;
@@ -275,35 +287,15 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
                 }
                 tmem_fence_after();
                 const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + buf * kAccStride;
-                // Z[k] (a rows) and Z[256 - k] (b rows); slot 0: Z[0], Z[128]
-                const size_t zoff = (size_t)(is_b ? (k ? kRingLen - k : kSlots) : k) * w.zw;
-                // a row: u = sum u a, v = sum v a; b row: u = sum u b, v = sum v b.
-                // The a row writes Z[k] = (sum u a, sum u b), the b row
-                // Z[256-k] = (sum v b, sum v a): each needs one value of its
-                // partner lane, so one shuffle per reference carries it (the
-                // b row sends u, the a row sends v); slot 0, whose (F[0],
-                // F[128]) products combine all four sums, exchanges both.
-                float2* const zrow = zbase + zoff;
+                float2* const zrow = zbase + (size_t)k * 2 * w.zw;
                 auto write_chunk = [&](const float (&r)[16], unsigned c) {
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
-                        const float u = r[2 * j], v = r[2 * j + 1];
-                        float2 zv;
-                        if (k == 0) {
-                            const float pu = __shfl_xor_sync(0xffffffffu, u, 1);
-                            const float pv = __shfl_xor_sync(0xffffffffu, v, 1);
-                            const float a1 = is_b ? pu : u, a4 = is_b ? pv : v;
-                            const float a2 = is_b ? u : pu, a3 = is_b ? v : pv;
-                            const float p1 = 0.25f * (a1 + a2 + a3 + a4);
-                            const float p2 = 0.25f * (a1 - a2 + a3 - a4);
-                            zv = is_b ? make_float2(p2, p2) : make_float2(p1, p1);
-                        } else {
-                            const float other = __shfl_xor_sync(0xffffffffu, is_b ? u : v, 1);
-                            zv = make_float2(is_b ? v : u, other);
-                        }
                         const unsigned ql = 8 * c + j;
-                        if (row_ok && ql < nq)
-                            __stcs(zrow + ql * zq, zv); // streamed: read back only by the next kernel
+                        if (row_ok && ql < nq &&
+                            GPUISAC_IN_BOUNDS(kChkMmaZ, (size_t)(zrow + ql * zq - w.z),
+                                              (size_t)w.n_part * w.n_ref * w.n_blocks * kRingLen * w.zw))
+                            __stcs(zrow + ql * zq, make_float2(r[2 * j], r[2 * j + 1])); // streamed: read once
                     }
                 };
                 if (nj) {
@@ -371,7 +363,7 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
     const unsigned gthreads = 16 * groups;
     const bool ctl = threadIdx.x >= zfft_group_threads(groups);
     const size_t unit_elems = (size_t)kRingLen * w.zw;
-    float2* const zb = reinterpret_cast<float2*>(smem_raw);                                // [256][zw]
+    float2* const zb = reinterpret_cast<float2*>(smem_raw);                                // [128][zw][a, b]
     float2* const wsp = reinterpret_cast<float2*>(smem_raw + zfft_zbuf_bytes(w.zw));       // [groups][kPairStride]
     float2* const tw = wsp + (size_t)groups * kPairStride;                                 // [16][kTwRow]
     PeakSlot* const slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);                 // [kZfftRing][64]
@@ -416,9 +408,12 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
                 return; // failure-path test: no copies
             const unsigned item = unit_item(u), b = u % w.n_blocks;
             const uint32_t bytes = (uint32_t)(unit_elems * sizeof(float2));
+            const size_t at = ((size_t)item * w.n_blocks + b) * unit_elems;
+            if (!GPUISAC_IN_BOUNDS(kChkZfftZ, at + unit_elems - 1, (size_t)n_items * w.n_blocks * unit_elems))
+                return; // (checked build) the groups' bounded wait reports the failure
             fence_proxy_async();
             mbar_expect_tx(full, bytes);
-            bulk_g2s(zb, w.z + ((size_t)item * w.n_blocks + b) * unit_elems, bytes, full);
+            bulk_g2s(zb, w.z + at, bytes, full);
         };
         // the groups' parked bests of a finished item, reduced in the
         // reference's order (better(); equal entries: the lower group, which
@@ -459,8 +454,10 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
                 const float bx = w.base ? w.base[pg].x : 0.f, by = w.base ? w.base[pg].y : 0.f;
                 const float2 sf = w.shifts_f[sidx];
                 const size_t o = (size_t)q * w.p_total + pg;
-                w.d_out[o] = ps.v;
-                w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+                if (GPUISAC_IN_BOUNDS(kChkZfftOut, o, (size_t)w.n_ref * w.p_total)) {
+                    w.d_out[o] = ps.v;
+                    w.peak_out[o] = make_float4(angle, bx + sf.x, by + sf.y, mirror ? 1.f : 0.f);
+                }
             }
         };
         bool failed = false;
@@ -526,9 +523,31 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
         const bool has = (unsigned)g < nsb; // group-uniform
         float2 x[16];
         if (has) {
+            // the ring sums e = (ua, va, ub, vb) of slot l + 16 m (m < 8) give
+            // Z[k] = (ua, ub) for k = l + 16 m (input m) and Z[256 - k] =
+            // (vb, va), input 15 - m of lane (16 - l) mod 16; lane 0 keeps
+            // its own: Z[256 - 16 m] is its input 16 - m, and slot 0 (the
+            // real (F[0], F[128]) products) gives Z[0] and Z[128]
+            const float4* z4 = reinterpret_cast<const float4*>(zb);
+            const int partner = (16 - l) & 15;
+            float p2 = 0.f;
 #pragma unroll
-            for (int m = 0; m < 16; m++)
-                x[m] = zb[(l + 16 * m) * w.zw + g];
+            for (int m = 0; m < 8; m++) {
+                const float4 e = z4[(l + 16 * m) * w.zw + g];
+                x[m] = make_float2(e.x, e.z);
+                x[15 - m] = make_float2(__shfl_sync(gmask, e.w, partner, 16), __shfl_sync(gmask, e.y, partner, 16));
+                if (l == 0) {
+                    if (m == 0) {
+                        const float p1 = 0.25f * (e.x + e.z + e.w + e.y);
+                        p2 = 0.25f * (e.x - e.z + e.w - e.y);
+                        x[0] = make_float2(p1, p1);
+                    } else {
+                        x[16 - m] = make_float2(e.w, e.y);
+                    }
+                }
+            }
+            if (l == 0)
+                x[8] = make_float2(p2, p2);
         }
         mbar_arrive(empty);
         if (has)
@@ -550,6 +569,8 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
 }
 
 // ============================================================================
+
+GPUISAC_CHECKED_READER(checked_read_split)
 
 static int device_sms()
 {

@@ -8,6 +8,50 @@
 
 namespace gpuisac {
 
+// ---------------------------------------------------------------------------
+// Checked build (-DGPUISAC_CHECKED): a guarded global access first tests its
+// element (or byte) index against the extent the kernel was given; a failing
+// access is skipped and recorded -- a count and the first (site, index) -- in
+// this translation unit's device words, never trapped.  The host reads and
+// clears them with the translation unit's reader (GPUISAC_CHECKED_READER,
+// collected by gpuisac_checked_failures).  In the normal build the guard is
+// the constant true.
+#ifdef GPUISAC_CHECKED
+static __device__ unsigned g_chk_count;
+static __device__ unsigned long long g_chk_first;
+__device__ __forceinline__ bool chk_in_bounds(unsigned site, unsigned long long i, unsigned long long n)
+{
+    if (i < n)
+        return true;
+    if (atomicAdd(&g_chk_count, 1u) == 0u)
+        g_chk_first = ((unsigned long long)site << 48) | (i & 0xFFFFFFFFFFFFull);
+    return false;
+}
+#define GPUISAC_IN_BOUNDS(site, i, n) \
+    (::gpuisac::chk_in_bounds((site), (unsigned long long)(i), (unsigned long long)(n)))
+#define GPUISAC_CHECKED_READER(fn)                                                        \
+    void fn(unsigned& count, unsigned long long& first)                                    \
+    {                                                                                      \
+        cudaMemcpyFromSymbol(&count, g_chk_count, sizeof(count));                          \
+        cudaMemcpyFromSymbol(&first, g_chk_first, sizeof(first));                          \
+        const unsigned zero = 0;                                                           \
+        cudaMemcpyToSymbol(g_chk_count, &zero, sizeof(zero));                              \
+    }
+#else
+#define GPUISAC_IN_BOUNDS(site, i, n) true
+#define GPUISAC_CHECKED_READER(fn)                                                        \
+    void fn(unsigned& count, unsigned long long& first)                                    \
+    {                                                                                      \
+        count = 0;                                                                         \
+        first = 0;                                                                         \
+    }
+#endif
+// guarded sites (the high 16 bits of a recorded failure)
+enum {
+    kChkSpectraOut = 1, kChkSpectraTmpl, kChkOperandOut, kChkMmaZ, kChkMmaA, kChkMmaB, kChkZfftZ, kChkZfftOut,
+    kChkMergeOut, kChkCcfRow, kChkR512Out, kChkR512Row, kChkR512Res
+};
+
 constexpr int kRingLen = 256;        // polar samples per ring (angles)
 constexpr int kSlots = kRingLen / 2; // spectrum slots per ring: k = 1..127, slot 0 = (F[0], F[128])
 constexpr int kFftGroup = 16;        // threads per 256-point FFT

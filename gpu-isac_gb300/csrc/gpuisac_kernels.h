@@ -289,4 +289,11 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
                             const float2* base, float* d_out, float4* peak_out, unsigned* err,
                             cudaStream_t stream, unsigned rule = kPeakMref);
 
+// the checked build's failure records of each instrumented translation unit
+// (count and first (site, index); read and cleared), zero in the normal build
+void checked_read_spectra(unsigned& count, unsigned long long& first);
+void checked_read_split(unsigned& count, unsigned long long& first);
+void checked_read_ccf(unsigned& count, unsigned long long& first);
+void checked_read_ring512(unsigned& count, unsigned long long& first);
+
 } // namespace gpuisac

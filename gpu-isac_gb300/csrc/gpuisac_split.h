@@ -35,7 +35,7 @@ struct SplitPlan {
 struct SplitMmaWork {
     const unsigned char* sop; // subject operand tiles [n_part x n_blocks][kSlots][sop_slot]
     const unsigned char* rop; // reference operand tiles [n_rtiles][kSlots][rop_slot]
-    float2* z;                // pair spectra [n_part][n_ref][n_blocks][256][zw]
+    float2* z;                // ring sums [n_part][n_ref][n_blocks][128 slots][zw][a|b] of (sum u, sum v)
     unsigned n_part, n_blocks, block, n_shift;
     unsigned n_ref, rblock, n_rtiles;
     unsigned kg, rga, rgb, n_cols, n_stages, zw;

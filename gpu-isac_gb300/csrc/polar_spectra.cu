@@ -113,7 +113,9 @@ polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const f
     float s1 = 0.f, s2 = 0.f;
 #pragma unroll 8
     for (unsigned r = 0; r < ring_num; r++) {
-        float2 o = __ldg(&tmpl[r * kRingLen + tid]);
+        const float2 o = GPUISAC_IN_BOUNDS(kChkSpectraTmpl, r * kRingLen + tid, ring_num * kRingLen)
+                             ? __ldg(&tmpl[r * kRingLen + tid])
+                             : make_float2(0.f, 0.f);
         float x = cnt_x + o.x;
         float y = (yoff + cnt_y) + o.y;
         float v = tex_objs ? tex2D<float>(tobj, x, y) : tex_sample(st, place, x, y);
@@ -199,8 +201,11 @@ polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const f
                 oa[i] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
                 ob[i] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
             } else {
-                out_row[ra * kSlots + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
-                if (has_b)
+                const size_t n_out = (size_t)n_img * n_shift * ring_num * kSlots;
+                const size_t at = (size_t)row * ring_num * kSlots + ra * kSlots + k;
+                if (GPUISAC_IN_BOUNDS(kChkSpectraOut, at, n_out))
+                    out_row[ra * kSlots + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
+                if (has_b && GPUISAC_IN_BOUNDS(kChkSpectraOut, at + kSlots, n_out))
                     out_row[rb * kSlots + k] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
             }
         }
@@ -247,6 +252,9 @@ polar_spectra_body(const StackDesc& st, const float2* __restrict__ tmpl, const f
             bl[j] = l0 | (l1 << 16);
         }
         unsigned char* p = tb + k * sb + kgi * kb;
+        const size_t n_tiles = is_ref ? (n_img + opnd.block - 1) / opnd.block : (size_t)n_img * opnd.n_blocks;
+        if (!GPUISAC_IN_BOUNDS(kChkOperandOut, (size_t)(p - opnd.base) + hb + 31, n_tiles * opnd.tile_bytes()))
+            continue;
         *reinterpret_cast<uint4*>(p) = make_uint4(ah[0], ah[1], ah[2], ah[3]);
         *reinterpret_cast<uint4*>(p + 16) = make_uint4(bh[0], bh[1], bh[2], bh[3]);
         *reinterpret_cast<uint4*>(p + hb) = make_uint4(al[0], al[1], al[2], al[3]);
@@ -296,6 +304,8 @@ polar_operands_kernel(StackDesc st, const float2* __restrict__ tmpl, const float
     polar_spectra_body<true>(st, tmpl, twiddle, ring_num, shift_int, n_shift, base, img0, n_img, is_ref, nullptr,
                              nullptr, tex_objs, opnd, blockIdx.x);
 }
+
+GPUISAC_CHECKED_READER(checked_read_spectra)
 
 cudaError_t launch_polar_spectra(const StackDesc& st, const float2* tmpl, const float2* twiddle,
                                  unsigned ring_num, const int2* shift_int, unsigned n_shift,

@@ -156,8 +156,11 @@ polar_spectra512_kernel(StackDesc st, const float2* __restrict__ tmpl, const flo
                 fa = make_float2(z.x, zn.x);
                 fb = make_float2(z.y, zn.y);
             }
-            out_row[ra * kS + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
-            if (has_b)
+            const size_t n_out = (size_t)n_img * n_shift * ring_num * kS;
+            const size_t at = (size_t)row * ring_num * kS + ra * kS + k;
+            if (GPUISAC_IN_BOUNDS(kChkR512Out, at, n_out))
+                out_row[ra * kS + k] = make_float2(wa * (fa.x + fa.y), wa * (fa.x - fa.y));
+            if (has_b && GPUISAC_IN_BOUNDS(kChkR512Out, at + kS, n_out))
                 out_row[rb * kS + k] = make_float2(wb * (fb.x + fb.y), wb * (fb.x - fb.y));
         }
         __syncwarp(gmask);
@@ -220,8 +223,12 @@ ccf_peak512_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__
             const float2* row = sp + (size_t)(s0 + g) * ring_num * kS + tid;
             float a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f;
 #pragma unroll 4
+            const size_t row_at = ((size_t)p * n_shift + s0 + g) * ring_num * kS + tid;
             for (unsigned r = 0; r < ring_num; r++) {
-                const float2 sv = __ldg(row + (size_t)r * kS);
+                const float2 sv = GPUISAC_IN_BOUNDS(kChkR512Row, row_at + (size_t)r * kS,
+                                                    (size_t)n_part * n_shift * ring_num * kS)
+                                      ? __ldg(row + (size_t)r * kS)
+                                      : make_float2(0.f, 0.f);
                 const float2 rv = refs[r * kS + tid];
                 a1 = fmaf(rv.x, sv.x, a1);
                 a2 = fmaf(rv.x, sv.y, a2);
@@ -321,8 +328,10 @@ ccf_peak512_kernel(const float2* __restrict__ sbj_sp, const float2* __restrict__
         const float byv = base ? base[pg].y : 0.f;
         const float2 sf = shifts_f[sidx];
         const size_t o = (size_t)q * p_total + pg;
-        d_out[o] = ps.v;
-        peak_out[o] = make_float4(angle, bxv + sf.x, byv + sf.y, mirror ? 1.f : 0.f);
+        if (GPUISAC_IN_BOUNDS(kChkR512Res, o, (size_t)n_ref * p_total)) {
+            d_out[o] = ps.v;
+            peak_out[o] = make_float4(angle, bxv + sf.x, byv + sf.y, mirror ? 1.f : 0.f);
+        }
     }
 }
 
@@ -337,6 +346,8 @@ size_t ccf512_smem(unsigned ring_num)
 }
 
 } // namespace
+
+GPUISAC_CHECKED_READER(checked_read_ring512)
 
 cudaError_t launch_polar_spectra512(const StackDesc& st, const float2* tmpl, const float2* tw512, unsigned ring_num,
                                     const int2* shift_int, unsigned n_shift, const float2* base, unsigned img0,

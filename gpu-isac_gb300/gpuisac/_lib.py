@@ -12,7 +12,8 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG_ROOT = os.path.dirname(HERE)
-LIB_PATH = os.path.join(PKG_ROOT, "lib", "libgpu_aln_pack.so")
+# GPUISAC_LIBRARY: another build of the library (the bounds-checked one)
+LIB_PATH = os.environ.get("GPUISAC_LIBRARY") or os.path.join(PKG_ROOT, "lib", "libgpu_aln_pack.so")
 
 
 class AlignConfig(ctypes.Structure):
@@ -49,7 +50,7 @@ EXPORTS = (
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
     "gpuisac_ref_free_averages", "gpuisac_set_contraction", "gpuisac_get_contraction", "gpuisac_test_stall_ccf", "gpuisac_normalize_mask",
-    "gpuisac_split_plan", "gpuisac_groups_stats",
+    "gpuisac_split_plan", "gpuisac_groups_stats", "gpuisac_checked_failures",
 )
 
 
@@ -136,6 +137,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_multi_ref_align_groups_device.restype = ctypes.c_int
     L.gpuisac_groups_stats.argtypes = [ctypes.POINTER(GpuisacGroupStats)]
     L.gpuisac_groups_stats.restype = ctypes.c_int
+    L.gpuisac_checked_failures.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
+    L.gpuisac_checked_failures.restype = ctypes.c_int
     vp, ci, cl, cf, cu = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_float, ctypes.c_uint
     L.gpuisac_align_proposals_device.argtypes = [aln_cfg_ptr, vp, vp, vp, vp, cu, vp, cu, vp, vp, vp]
     L.gpuisac_nn_features.argtypes = [vp, cu, cu, cu, vp, vp, vp, vp]

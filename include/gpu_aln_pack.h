@@ -240,6 +240,15 @@ int gpuisac_multi_ref_align_groups_device(const AlignConfig *cfg, const GpuisacG
                                           const float *base_shift, float *d_out, float *peak_out,
                                           void *stream);
 
+/* No counterpart in the reference (its only checks are cudaGetLastError
+ * after each launch).  In a library built with -DGPUISAC_CHECKED
+ * (gpu-isac_gb300/build.py --checked), every guarded global access of the spectra, contraction, FFT
+ * and peak kernels tests its index against the extent the kernel was given
+ * and skips (and records) an access outside it.  Returns the number of
+ * accesses skipped since the last call (and clears the records), the first
+ * one's (site << 48 | index) in *first; -1 in a normal build. */
+int gpuisac_checked_failures(unsigned long long *first);
+
 /* What the last gpuisac_multi_ref_align_groups_device call of the process
  * did: host milliseconds from entry to its tables and texture objects being
  * uploaded (plan_ms), milliseconds recording and instantiating a new launch
