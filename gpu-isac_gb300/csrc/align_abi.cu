@@ -226,8 +226,30 @@ struct Workspace {
     TexStack ref_tex, sbj_tex; // the stacks as textures for the texture unit
     cudaStream_t copy_stream = nullptr; // results to the host, overlapping the next chunk
     cudaEvent_t chunk_done[2] = {nullptr, nullptr};
+    // tensor-core path: contraction and FFT on a high-priority stream, the next
+    // chunk's operand kernel on a low-priority one (events between them)
+    cudaStream_t split_hi = nullptr, split_lo = nullptr;
+    cudaEvent_t ops_done[2] = {nullptr, nullptr}, mma_done[2] = {nullptr, nullptr};
+    cudaEvent_t split_entry = nullptr, split_exit = nullptr;
     void release()
     {
+        for (int i = 0; i < 2; i++) {
+            if (ops_done[i])
+                cudaEventDestroy(ops_done[i]);
+            if (mma_done[i])
+                cudaEventDestroy(mma_done[i]);
+            ops_done[i] = mma_done[i] = nullptr;
+        }
+        if (split_entry)
+            cudaEventDestroy(split_entry);
+        if (split_exit)
+            cudaEventDestroy(split_exit);
+        split_entry = split_exit = nullptr;
+        if (split_hi)
+            cudaStreamDestroy(split_hi);
+        if (split_lo)
+            cudaStreamDestroy(split_lo);
+        split_hi = split_lo = nullptr;
         for (int i = 0; i < 2; i++) {
             if (chunk_done[i])
                 cudaEventDestroy(chunk_done[i]);
@@ -416,6 +438,24 @@ int prepare_copy_back(Workspace& ws)
 // The same alignment with the contraction on the tensor cores: reference
 // operands once, then per particle chunk the subject operands, the MMA kernel
 // (pair spectra to HBM) and the inverse-FFT / peak kernel.
+// the tensor-core path's streams and events (created once per workspace)
+int prepare_split_streams(Workspace& ws)
+{
+    if (ws.split_hi)
+        return 0;
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&ws.split_hi, cudaStreamNonBlocking, greatest));
+    CK(cudaStreamCreateWithPriority(&ws.split_lo, cudaStreamNonBlocking, least));
+    for (int i = 0; i < 2; i++) {
+        CK(cudaEventCreateWithFlags(&ws.ops_done[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ws.mma_done[i], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&ws.split_entry, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ws.split_exit, cudaEventDisableTiming));
+    return 0;
+}
+
 int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs, const StackDesc& sbjs,
                         const unsigned long long* ref_tx, const unsigned long long* sbj_tx, const float2* d_base,
                         float* d_out, float4* d_peak, float mem_request, cudaStream_t st, const HostOut* host)
@@ -428,48 +468,69 @@ int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs,
     }
     if (ws.rop.ensure(split_rop_bytes(pl)))
         return E_NOMEM;
-    cudaEvent_t ev = g_timer.begin(st);
+    int rc = prepare_split_streams(ws);
+    if (rc)
+        return rc;
+    // work of the call: the contraction and the FFT on `hi`, the particle
+    // operands on `lo` -- a lower priority, so that one operand CTA shares each
+    // SM with the contraction's persistent CTA instead of delaying it (575.7
+    // -> 559.5 ms per 50,000 x 200 step) -- both after the caller's earlier
+    // work on st, and st after both
+    cudaStream_t hi = ws.split_hi, lo = ws.split_lo;
+    CK(cudaEventRecord(ws.split_entry, st));
+    CK(cudaStreamWaitEvent(hi, ws.split_entry, 0));
+    CK(cudaStreamWaitEvent(lo, ws.split_entry, 0));
+    cudaEvent_t ev = g_timer.begin(hi);
     CK(launch_polar_operands(refs, ws.tmpl.p, ws.tw.p, g.NR, ws.zero_shift.p, 1, nullptr, 0, g.R, 1,
-                             split_ref_layout(pl, ws.rop.p), st, ref_tx));
-    g_timer.end(K_SPECTRA, ev, st);
-    // particle chunk: operands and pair spectra of a particle (21 MB at 76²,
-    // 35 rings, 49 shifts, 200 references) within the requested share of
-    // free memory, at most 2,048 particles
+                             split_ref_layout(pl, ws.rop.p), hi, ref_tx));
+    g_timer.end(K_SPECTRA, ev, hi);
+    // particle chunk: two operand buffers and the pair spectra of a particle
+    // (4.2 + 19.6 MB at 76², 35 rings, 49 shifts, 200 references) within the
+    // requested share of free memory, at most 2,048 particles
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     const double frac = (mem_request > 0.f && mem_request <= 1.f) ? mem_request : 0.9;
     const size_t budget = (size_t)((double)free_b * frac) / 2;
-    const size_t per_part = split_sop_bytes(pl, 1) + split_z_bytes(pl, 1, g.R);
+    const size_t per_part = 2 * split_sop_bytes(pl, 1) + split_z_bytes(pl, 1, g.R);
     size_t chunk = std::max<size_t>(1, std::min<size_t>(budget / per_part, 2048));
     chunk = std::min<size_t>(chunk, g.P);
-    if (ws.sop.ensure(split_sop_bytes(pl, (unsigned)chunk)) ||
-        ws.zsp.ensure(split_z_bytes(pl, (unsigned)chunk, g.R) / sizeof(float2)) || ws.err.ensure(1))
+    const size_t sop_bytes = split_sop_bytes(pl, (unsigned)chunk);
+    if (ws.sop.ensure(2 * sop_bytes) || ws.zsp.ensure(split_z_bytes(pl, (unsigned)chunk, g.R) / sizeof(float2)) ||
+        ws.err.ensure(1))
         return E_NOMEM;
-    CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), hi));
     if (host) {
-        int rc = prepare_copy_back(ws);
+        rc = prepare_copy_back(ws);
         if (rc)
             return rc;
     }
-    const OperandLayout sl = split_sbj_layout(pl, ws.sop.p);
-    unsigned prev_p0 = 0, prev_n = 0, slot = 0;
-    for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk) {
+    unsigned prev_p0 = 0, prev_n = 0, slot = 0, c = 0;
+    for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk, c++) {
         const unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
-        ev = g_timer.begin(st);
-        CK(launch_polar_operands(sbjs, ws.tmpl.p, ws.tw.p, g.NR, ws.shifts_i.p, g.S, d_base, p0, n, 0, sl, st,
-                                 sbj_tx));
-        g_timer.end(K_SPECTRA, ev, st);
-        ev = g_timer.begin(st);
-        CK(launch_ccf_mma(pl, ws.sop.p, ws.rop.p, ws.zsp.p, n, g.R, g.S, ws.err.p, st));
-        g_timer.end(K_MMA, ev, st);
-        ev = g_timer.begin(st);
+        const unsigned buf = c & 1u;
+        unsigned char* const sop = ws.sop.p + buf * sop_bytes;
+        // operands of chunk c into buffer c mod 2, once the contraction of
+        // chunk c - 2 has read it
+        if (c >= 2)
+            CK(cudaStreamWaitEvent(lo, ws.mma_done[buf], 0));
+        ev = g_timer.begin(lo);
+        CK(launch_polar_operands(sbjs, ws.tmpl.p, ws.tw.p, g.NR, ws.shifts_i.p, g.S, d_base, p0, n, 0,
+                                 split_sbj_layout(pl, sop), lo, sbj_tx));
+        g_timer.end(K_SPECTRA, ev, lo);
+        CK(cudaEventRecord(ws.ops_done[buf], lo));
+        CK(cudaStreamWaitEvent(hi, ws.ops_done[buf], 0));
+        ev = g_timer.begin(hi);
+        CK(launch_ccf_mma(pl, sop, ws.rop.p, ws.zsp.p, n, g.R, g.S, ws.err.p, hi));
+        g_timer.end(K_MMA, ev, hi);
+        CK(cudaEventRecord(ws.mma_done[buf], hi));
+        ev = g_timer.begin(hi);
         CK(launch_zfft_peak(pl, ws.zsp.p, n, p0, g.P, g.R, g.S, ws.tw.p, ws.shifts_f.p, d_base, d_out, d_peak,
-                            ws.err.p, st));
-        g_timer.end(K_ZFFT, ev, st);
+                            ws.err.p, hi));
+        g_timer.end(K_ZFFT, ev, hi);
         if (host) {
-            CK(cudaEventRecord(ws.chunk_done[slot], st));
+            CK(cudaEventRecord(ws.chunk_done[slot], hi));
             if (prev_n) {
-                int rc = copy_chunk_back(g, ws, host, d_out, d_peak, prev_p0, prev_n, ws.chunk_done[slot ^ 1u]);
+                rc = copy_chunk_back(g, ws, host, d_out, d_peak, prev_p0, prev_n, ws.chunk_done[slot ^ 1u]);
                 if (rc)
                     return rc;
             }
@@ -478,8 +539,11 @@ int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs,
         prev_n = n;
         slot ^= 1u;
     }
+    // every operand launch precedes a contraction on hi: hi's end is the call's end
+    CK(cudaEventRecord(ws.split_exit, hi));
+    CK(cudaStreamWaitEvent(st, ws.split_exit, 0));
     if (host && prev_n) {
-        int rc = copy_chunk_back(g, ws, host, d_out, d_peak, prev_p0, prev_n, ws.chunk_done[slot ^ 1u]);
+        rc = copy_chunk_back(g, ws, host, d_out, d_peak, prev_p0, prev_n, ws.chunk_done[slot ^ 1u]);
         if (rc)
             return rc;
         CK(cudaStreamSynchronize(ws.copy_stream));
@@ -487,9 +551,6 @@ int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs,
     return 0;
 }
 
-// Device-resident multi-reference alignment of P particles against R refs.
-// With host destinations, each chunk's columns are copied back on a second
-// stream while the next chunk computes.
 // 512-sample rings (ring512.cu): FP32 contraction whatever the mode; chunks
 // of particles bounded by the memory request, results copied to the host at
 // the end when `host` is given

@@ -145,34 +145,36 @@ __device__ __forceinline__ void fft_peak_regs(float2 (&x)[16], float2* gz, const
     // group-uniform, NaN inputs included
     vm[0] = __shfl_sync(gmask, vm[0], 0, 16);
     vm[1] = __shfl_sync(gmask, vm[1], 0, 16);
+    // this transform's better mirror in the reference's order (at equal
+    // maxima the normal one: its scan index is lower), then against the
+    // running best -- the same result as offering both in turn, with one
+    // index search and one gather of the neighbours
+    const bool mir = vm[1] > vm[0] || vm[0] != vm[0];
+    const float v = mir ? vm[1] : vm[0];
+    if (!(v >= st.bv))
+        return;
+    unsigned t = 0xffffffffu;
 #pragma unroll
-    for (int mir = 0; mir < 2; mir++) {
-        const float v = vm[mir];
-        if (!(v >= st.bv))
-            continue;
-        unsigned t = 0xffffffffu;
+    for (int k2 = 15; k2 >= 0; k2--)
+        if ((mir ? x[perm16(k2)].y : x[perm16(k2)].x) == v)
+            t = l + 16 * k2;
 #pragma unroll
-        for (int k2 = 15; k2 >= 0; k2--)
-            if ((mir ? x[perm16(k2)].y : x[perm16(k2)].x) == v)
-                t = l + 16 * k2;
+    for (int off = 8; off > 0; off >>= 1)
+        t = min(t, __shfl_xor_sync(gmask, t, off));
+    t = __shfl_sync(gmask, t, 0, 16);
+    const unsigned hc = mir ? n_shift + s : s;
+    if (t < (unsigned)kRingLen && better(v, hc, t, st.bv, st.bh, st.bt)) {
+        st.bv = v;
+        st.bh = hc;
+        st.bt = t;
+        __syncwarp(gmask);
 #pragma unroll
-        for (int off = 8; off > 0; off >>= 1)
-            t = min(t, __shfl_xor_sync(gmask, t, off));
-        t = __shfl_sync(gmask, t, 0, 16);
-        const unsigned hc = mir ? n_shift + s : s;
-        if (t < (unsigned)kRingLen && better(v, hc, t, st.bv, st.bh, st.bt)) {
-            st.bv = v;
-            st.bh = hc;
-            st.bt = t;
-            __syncwarp(gmask);
-#pragma unroll
-            for (int k2 = 0; k2 < 16; k2++)
-                wf[l + 16 * k2] = mir ? x[perm16(k2)].y : x[perm16(k2)].x;
-            __syncwarp(gmask);
-            if (l < 7)
-                st.nb = wf[(t + (unsigned)l - 3u) & (kRingLen - 1)];
-            __syncwarp(gmask);
-        }
+        for (int k2 = 0; k2 < 16; k2++)
+            wf[l + 16 * k2] = mir ? x[perm16(k2)].y : x[perm16(k2)].x;
+        __syncwarp(gmask);
+        if (l < 7)
+            st.nb = wf[(t + (unsigned)l - 3u) & (kRingLen - 1)];
+        __syncwarp(gmask);
     }
 }
 
