@@ -250,9 +250,12 @@ LEARNED_AS_WRITTEN = dict(LEARNED, workload="learned_100000x76_500ref_as_written
 # the headline workload with the learned proposal in front: the chosen form
 # (evaluation particles = the workload's own, training particles an
 # independent draw of the same generator)
+# (k = 16: 4.2x the plain search at 99.56 % same best with a 3e-3 margin
+# calibration, against 3.1x at k = 32; the margin is calibrated to 2e-3 here
+# to keep a wider distance from the 99.5 % bar)
 LEARNED_MREF = dict(workload="learned_mref_50000x76_200ref", synth_idx=1, particles=None, refs=200,
-                    train_alignments=50000, img_dim=76, rings=35, shift_range=3, n_shifts=49, snr=0.05, k=32,
-                    max_wrong=3e-3)
+                    train_alignments=50000, img_dim=76, rings=35, shift_range=3, n_shifts=49, snr=0.05, k=16,
+                    max_wrong=2e-3)
 # the large-box workload with the learned proposal in front (evaluation
 # particles = the workload's own, training particles an independent draw)
 LEARNED_LARGEBOX = dict(workload="largebox_learned_x128_500ref", synth_idx=4, particles=None, refs=500,
@@ -1113,9 +1116,9 @@ def bench_ours(args):
     chosen = None
     if rank == 0 and world == 1 and not args.no_learned and WORKLOAD["workload"].startswith("mref"):
         blk = bench_learned(args, dev, L, LEARNED_MREF, resident=(st, parts_d, refs_d))
-        chosen = {"form": "learned reference proposal (network inference on the tensor cores, top-32 references) "
-                          "+ exhaustive shift x angle x mirror search of every proposal, full search of every "
-                          "reference below the calibrated margin",
+        chosen = {"form": f"learned reference proposal (network inference on the tensor cores, top-{LEARNED_MREF['k']} "
+                          "references) + exhaustive shift x angle x mirror search of every proposal, full search of "
+                          "every reference below the calibrated margin",
                   "value": blk["value"], "unit": UNIT, "ms_per_step": blk["ms_per_step"],
                   "ratio_vs_plain_fp32": blk["ratio_vs_plain_fp32"], "plain_fp32": blk["plain_fp32"],
                   "vs_fp64_oracle": blk["vs_fp64_oracle"],

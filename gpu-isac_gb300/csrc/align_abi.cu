@@ -642,7 +642,7 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
     chunk = std::min<size_t>(chunk, g.P);
     if (ws.sbj_sp.ensure(per_part / sizeof(float2) * chunk))
         return E_NOMEM;
-    if (ws.err.ensure(1))
+    if (ws.err.ensure(2)) // the timeout flag and the CCF kernel's work counter
         return E_NOMEM;
     CK(cudaMemsetAsync(ws.err.p, 0, sizeof(unsigned), st));
     // a chunk's results to the host, on the copy stream after its kernels
@@ -672,7 +672,7 @@ int run_alignment(const AlignConfig* cfg, const Geometry& g, Workspace& ws, cons
         g_timer.end(K_SPECTRA, ev, st);
         ev = g_timer.begin(st);
         CK(launch_ccf_peak(ws.sbj_sp.p, ws.ref_sp.p, ws.tw.p, g.NR, g.S, g.R, n, p0, g.P, ws.shifts_f.p, d_base, d_out,
-                           d_peak, ws.err.p, st));
+                           d_peak, ws.err.p, st, kPeakMref, ws.err.p + 1));
         g_timer.end(K_CCF, ev, st);
         if (host)
             CK(cudaEventRecord(ws.chunk_done[slot], st));

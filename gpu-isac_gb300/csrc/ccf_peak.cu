@@ -338,6 +338,10 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
     uint64_t* bar = reinterpret_cast<uint64_t*>(slots + 16);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    // the item after the current one, by item parity: taken from the work
+    // counter (w.item_counter) by the contraction side's thread 0, read by
+    // both sides
+    volatile unsigned* next_item = reinterpret_cast<volatile unsigned*>(abort_flag + 1);
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
@@ -410,8 +414,10 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
         bool pending = false; // thread 0: copies in flight
         if (tid == 0)
             pending = issue(grp, pb, pe - pb, 0);
-        unsigned it = 0;
+        unsigned it = 0, ii = 0;
         while (!failed) {
+            if (tid == 0)
+                next_item[ii & 1u] = w.item_counter ? gridDim.x + atomicAdd(w.item_counter, 1u) : item + gridDim.x;
             // this item's references -> tensor memory (both halves read every ring)
             for (unsigned j = 2 * half; j < nrp; j += 2 * (NC / 128)) {
 #pragma unroll
@@ -434,7 +440,8 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             tmem_fence_after();
             CcfGroup ngrp;
             unsigned nq0 = 0, npb = 0, npe = 0;
-            const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
+            const unsigned nxt = next_item[ii & 1u];
+            const bool has_next = decode_item(w, nxt, QT, ngrp, nq0, npb, npe);
 
             const unsigned nrows = (pe - pb) * vstride;
             for (unsigned v0 = 0; v0 < nrows && !failed; v0 += NSI, it++) {
@@ -539,7 +546,8 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
             }
             if (failed || !has_next)
                 break;
-            item += gridDim.x;
+            item = nxt;
+            ii++;
             grp = ngrp;
             q0 = nq0;
             pb = npb;
@@ -564,11 +572,8 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
         // both buffers start empty
         nbar_arrive(kWsBarEmpty + 0, NT);
         nbar_arrive(kWsBarEmpty + 1, NT);
-        unsigned it = 0;
+        unsigned it = 0, ii = 0;
         while (!failed) {
-            CcfGroup ngrp;
-            unsigned nq0 = 0, npb = 0, npe = 0;
-            const bool has_next = decode_item(w, item + gridDim.x, QT, ngrp, nq0, npb, npe);
             // st: the slot's running best of particle pb + pc, the particle of
             // the shift group's first row.  In the group that holds pc's last
             // row, a slot whose row already belongs to pc + 1 parks its best
@@ -608,9 +613,16 @@ ccf_peak_ws_kernel(CcfWork w, const float2* __restrict__ twiddle, unsigned ring_
                     pc++;
                 }
             }
-            if (failed || !has_next)
+            if (failed)
                 break;
-            item += gridDim.x;
+            // (written by the contraction side before this item's first full buffer)
+            CcfGroup ngrp;
+            unsigned nq0 = 0, npb = 0, npe = 0;
+            const unsigned nxt = next_item[ii & 1u];
+            if (!decode_item(w, nxt, QT, ngrp, nq0, npb, npe))
+                break;
+            item = nxt;
+            ii++;
             grp = ngrp;
             q0 = nq0;
             pb = npb;
@@ -777,7 +789,7 @@ static size_t ws_smem_bytes(unsigned ring_num)
 {
     const unsigned nrp = 2 * ((ring_num + 1) / 2), nsi = ws_shifts_per_group(ring_num);
     return (size_t)nsi * nrp * kSlots * sizeof(float2) + 2 * nsi * 4 * kPairStride * sizeof(float2) +
-           16 * kTwRow * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16;
+           16 * kTwRow * sizeof(float2) + 16 * sizeof(PeakSlot) + 16 + 16; // barrier, tensor-memory slot, abort, next items
 }
 
 template <int CW, int NSI, int QR>
@@ -906,6 +918,13 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w_in, int variant, const float2*
     CcfWork w = w_in;
     ccf_test_settings(w.test_stall, w.wait_iters);
     const unsigned grid = persistent_grid(w.n_items, 1);
+    if (variant != kCcfWs)
+        w.item_counter = nullptr; // (the other kernels take items CTA + k x grid)
+    else if (w.item_counter) {
+        cudaError_t e = cudaMemsetAsync(w.item_counter, 0, sizeof(unsigned), stream);
+        if (e != cudaSuccess)
+            return e;
+    }
     if (variant == kCcfWs) {
         const bool four = ccf_tile(ring_num, n_shift, true).ws_warps == 4;
         const bool one_ref = w.max_ref == 1;
@@ -951,7 +970,7 @@ cudaError_t launch_ccf_peak_work(const CcfWork& w_in, int variant, const float2*
 cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const float2* twiddle, unsigned ring_num,
                             unsigned n_shift, unsigned n_ref, unsigned n_part, unsigned p_global0, unsigned p_total,
                             const float2* shifts_f, const float2* base, float* d_out, float4* peak_out,
-                            unsigned* err, cudaStream_t stream, unsigned rule)
+                            unsigned* err, cudaStream_t stream, unsigned rule, unsigned* item_counter)
 {
     if (n_part == 0 || n_ref == 0)
         return cudaSuccess;
@@ -979,6 +998,7 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
     g.rule = rule;
     w.n_items = g.ref_tiles * ((n_part + w.ppc - 1) / w.ppc);
     w.max_ref = n_ref;
+    w.item_counter = item_counter;
     return launch_ccf_peak_work(w, variant, twiddle, ring_num, n_shift, shifts_f, err, stream);
 }
 

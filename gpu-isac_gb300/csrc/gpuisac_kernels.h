@@ -234,6 +234,11 @@ struct CcfWork {
     unsigned n_groups;
     unsigned n_items;
     const unsigned* dyn;
+    // the warp-specialised kernel's work counter (device word, zeroed by the
+    // launcher): its CTAs take their next items from it, so that they stay
+    // together on the same particle blocks (their spectra read from L2 by
+    // every reference tile); null: item = CTA + k x grid
+    unsigned* item_counter;
     unsigned ppc;     // particles per work item
     unsigned max_ref; // most references of any group (0: not known); 1 selects the one-reference contraction
     // failure-path tests only (gpuisac_test_stall_ccf): the kernels that stage
@@ -287,7 +292,7 @@ cudaError_t launch_ccf_peak(const float2* sbj_sp, const float2* ref_sp, const fl
                             unsigned ring_num, unsigned n_shift, unsigned n_ref, unsigned n_part,
                             unsigned p_global0, unsigned p_total, const float2* shifts_f,
                             const float2* base, float* d_out, float4* peak_out, unsigned* err,
-                            cudaStream_t stream, unsigned rule = kPeakMref);
+                            cudaStream_t stream, unsigned rule = kPeakMref, unsigned* item_counter = nullptr);
 
 // the checked build's failure records of each instrumented translation unit
 // (count and first (site, index); read and cleared), zero in the normal build
