@@ -298,7 +298,7 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
     G_CK(S.shifts_f.ensure(Sn));
     G_CK(S.shifts_i.ensure(Sn));
     G_CK(S.zero.ensure(1));
-    G_CK(S.err.ensure(1));
+    G_CK(S.err.ensure(2)); // the timeout flag and the CCF kernels' work counter
 
     // spectra rows of each wave (the first also computes the reference rows)
     std::vector<size_t> wave_rows(W);
@@ -472,6 +472,7 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
             cw.n_groups = 1;
             cw.n_items = 0xFFFFFFFFu; // a grid over every SM; the items come from dyn
             cw.ppc = ppc;
+            cw.item_counter = S.err.p + 1;
             e = launch_ccf_peak_work(cw, tile.variant, S.tw.p, NR, Sn, S.shifts_f.p, S.err.p, cap);
         }
         cudaGraph_t graph = nullptr;

@@ -403,6 +403,7 @@ int run_iteration(MgState& s)
         w.n_items = cw.n_items;
         w.ppc = ppc;
         w.max_ref = 1; // one reference (the class average) per group
+        w.item_counter = s.err.p + 1; // (err holds the timeout flag and this counter)
         MG_CK(launch_ccf_peak_work(w, tile.variant, s.tw.p, NR, S, s.shifts_f.p, s.err.p, st));
     }
     s.h_peak.resize(P);
@@ -592,7 +593,7 @@ AlignParam* ref_free_alignment_2D_init(const AlignConfig* aln_cfg, const float**
               s.d.ensure(s.P) == cudaSuccess && s.tw.ensure(kRingLen) == cudaSuccess &&
               s.tmpl.ensure(geo.tmpl.size()) == cudaSuccess && s.ref_sp.ensure((size_t)s.R * row) == cudaSuccess &&
               s.base.ensure(s.P) == cudaSuccess && s.zero.ensure(1) == cudaSuccess &&
-              s.peak.ensure(s.P) == cudaSuccess && s.err.ensure(1) == cudaSuccess &&
+              s.peak.ensure(s.P) == cudaSuccess && s.err.ensure(2) == cudaSuccess &&
               s.cid.ensure(s.R + 1) == cudaSuccess && s.xf.ensure(s.P) == cudaSuccess;
     ok = ok && cudaMemcpy(s.tw.p, geo.tw.data(), kRingLen * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(s.tmpl.p, geo.tmpl.data(), geo.tmpl.size() * sizeof(float2), cudaMemcpyHostToDevice) ==

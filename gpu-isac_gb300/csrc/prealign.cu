@@ -239,7 +239,7 @@ AlignParam* pre_align_init(unsigned int num_particles, const AlignConfig* aln_cf
     const int2 zero = make_int2(0, 0);
     bool ok = s.sbj.ensure((size_t)s.capacity * img) == cudaSuccess && s.ref.ensure(img) == cudaSuccess &&
               s.tw.ensure(kRingLen) == cudaSuccess && s.tmpl.ensure(geo.tmpl.size()) == cudaSuccess &&
-              s.zero.ensure(1) == cudaSuccess && s.err.ensure(1) == cudaSuccess &&
+              s.zero.ensure(1) == cudaSuccess && s.err.ensure(2) == cudaSuccess &&
               s.ref_sp.ensure((size_t)geo.NR * kSlots) == cudaSuccess;
     // slots never fetched read as zero (the reference leaves them undefined)
     ok = ok && cudaMemset(s.sbj.p, 0, (size_t)s.capacity * img * sizeof(float)) == cudaSuccess &&
@@ -337,7 +337,7 @@ void pre_align_run(int start_idx, int stop_idx)
             PRE_CK(launch_polar_spectra(sbjs, s.tmpl.p, s.tw.p, g.NR, s.shifts_i.p, g.S, s.base.p, c0, c, 0,
                                         s.sbj_sp.p, st, nullptr, sbj_tx));
             PRE_CK(launch_ccf_peak(s.sbj_sp.p, s.ref_sp.p, s.tw.p, g.NR, g.S, 1, c, c0, n, s.shifts_f.p, s.base.p,
-                                   s.d.p, s.peak.p, s.err.p, st, kPeakPreAlign));
+                                   s.d.p, s.peak.p, s.err.p, st, kPeakPreAlign, s.err.p + 1));
         }
         s.h_peak.resize(n);
         PRE_CK(cudaMemcpyAsync(s.h_peak.data(), s.peak.p, n * sizeof(float4), cudaMemcpyDeviceToHost, st));

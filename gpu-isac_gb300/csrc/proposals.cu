@@ -103,7 +103,7 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
     P_CK(S.shifts_f.ensure(Sn));
     P_CK(S.shifts_i.ensure(Sn));
     P_CK(S.zero.ensure(1));
-    P_CK(S.err.ensure(1));
+    P_CK(S.err.ensure(2)); // the timeout flag and the CCF kernel's work counter
     P_CK(S.ref_sp.ensure(row_elems * geo.R));
     P_CK(S.table.ensure(n_sel));
     const int2 zero = make_int2(0, 0);
@@ -184,6 +184,7 @@ extern "C" int gpuisac_align_proposals_device(const AlignConfig* cfg, const floa
         w.n_groups = n;
         w.n_items = n * tiles;
         w.ppc = 1;
+        w.item_counter = S.err.p + 1;
         P_CK(launch_ccf_peak_work(w, variant, S.tw.p, NR, Sn, S.shifts_f.p, S.err.p, st));
     }
     P_CK(cudaStreamSynchronize(st)); // the host table must outlive its copies
@@ -311,7 +312,7 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
     P_CK(S.shifts_f.ensure(Sn));
     P_CK(S.shifts_i.ensure(Sn));
     P_CK(S.zero.ensure(1));
-    P_CK(S.err.ensure(1));
+    P_CK(S.err.ensure(2)); // the timeout flag and the CCF kernel's work counter
     P_CK(S.ref_sp.ensure(row_elems * R));
     const int2 zero = make_int2(0, 0);
     P_CK(cudaMemcpy(S.tw.p, geo.tw.data(), kRingLen * sizeof(float2), cudaMemcpyHostToDevice));
@@ -374,6 +375,7 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
         w.n_groups = n_groups;
         w.n_items = n_groups * tiles;
         w.ppc = 1;
+        w.item_counter = S.err.p + 1;
         P_CK(launch_ccf_peak_work(w, variant, S.tw.p, NR, Sn, S.shifts_f.p, S.err.p, st));
         return 0;
     };
