@@ -340,15 +340,18 @@ __global__ void __launch_bounds__(kMmaThreads, 1) ccf_mma_kernel(SplitMmaWork w,
 // inverse FFT + peak search of the pair spectra Z, one (particle, reference)
 // per work item, one 16-thread group per shift of a block (w.block groups, up
 // to kSplitMaxBlock = 49, in whole warps), plus one control warp.  The units
-// (item, shift block) stream through one shared Z buffer: the control warp
-// copies unit u + 1 in as soon as every group has taken its unit-u column into
-// registers (mbarrier `empty`), so the copy overlaps the FFTs; each group then
-// transforms in its own workspace and runs on without waiting for the others.
+// (item, shift block) stream through one shared buffer of ring sums in
+// kZfftParts parts (of 128 / kZfftParts slots each): the control warp copies a
+// part of unit u + 1 in as soon as every group has taken its values of that
+// part of unit u into registers (mbarriers `empty`), so several copies can be
+// in flight and they overlap the FFTs; each group then transforms in its own
+// workspace and runs on without waiting for the others.
 // A finished item's group bests are parked in one of kZfftRing slot sets
 // (mbarrier `parked`); the control warp merges them, writes the outputs and
 // hands the set back (mbarrier `freed`).
 constexpr int kZfftCtlThreads = 32;
 constexpr unsigned kZfftRing = 4;
+constexpr int kZfftParts = 2; // divides 8: a lane's 8 slots l + 16 m split evenly (4 parts: FFT kernel 261 -> 289 ms)
 __host__ __device__ constexpr unsigned zfft_group_threads(unsigned groups) { return (16 * groups + 31) / 32 * 32; }
 __host__ __device__ constexpr size_t zfft_zbuf_bytes(unsigned zw)
 {
@@ -367,9 +370,9 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
     float2* const wsp = reinterpret_cast<float2*>(smem_raw + zfft_zbuf_bytes(w.zw));       // [groups][kPairStride]
     float2* const tw = wsp + (size_t)groups * kPairStride;                                 // [16][kTwRow]
     PeakSlot* const slots = reinterpret_cast<PeakSlot*>(tw + 16 * kTwRow);                 // [kZfftRing][64]
-    uint64_t* const full = reinterpret_cast<uint64_t*>(slots + kZfftRing * 64);
-    uint64_t* const empty = full + 1;
-    uint64_t* const parked = full + 2;             // [kZfftRing]
+    uint64_t* const full = reinterpret_cast<uint64_t*>(slots + kZfftRing * 64); // [kZfftParts]
+    uint64_t* const empty = full + kZfftParts;     // [kZfftParts]
+    uint64_t* const parked = empty + kZfftParts;   // [kZfftRing]
     uint64_t* const freed = parked + kZfftRing;    // [kZfftRing]
     volatile int* const abort_flag = reinterpret_cast<volatile int*>(freed + kZfftRing);
 
@@ -383,8 +386,10 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
         tw[tl * kTwRow + tj] = make_float2(t.x, t.y * -1.f);
     }
     if (tid == 0) {
-        mbar_init(full, 1);
-        mbar_init(empty, gthreads);
+        for (int h = 0; h < kZfftParts; h++) {
+            mbar_init(full + h, 1);
+            mbar_init(empty + h, gthreads);
+        }
         for (unsigned i = 0; i < kZfftRing; i++) {
             mbar_init(parked + i, gthreads);
             mbar_init(freed + i, 1);
@@ -403,17 +408,18 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
     if (ctl) {
         // ---------------- control warp: copies, merges, outputs ----------------
         const int lane = tid & 31;
-        auto issue = [&](unsigned u) {
+        const size_t half = unit_elems / kZfftParts; // one part: [128 / kZfftParts][zw][a, b]
+        auto issue = [&](unsigned u, int h) {
             if (w.test_stall)
                 return; // failure-path test: no copies
             const unsigned item = unit_item(u), b = u % w.n_blocks;
-            const uint32_t bytes = (uint32_t)(unit_elems * sizeof(float2));
-            const size_t at = ((size_t)item * w.n_blocks + b) * unit_elems;
-            if (!GPUISAC_IN_BOUNDS(kChkZfftZ, at + unit_elems - 1, (size_t)n_items * w.n_blocks * unit_elems))
+            const uint32_t bytes = (uint32_t)(half * sizeof(float2));
+            const size_t at = ((size_t)item * w.n_blocks + b) * unit_elems + h * half;
+            if (!GPUISAC_IN_BOUNDS(kChkZfftZ, at + half - 1, (size_t)n_items * w.n_blocks * unit_elems))
                 return; // (checked build) the groups' bounded wait reports the failure
             fence_proxy_async();
-            mbar_expect_tx(full, bytes);
-            bulk_g2s(zb, w.z + at, bytes, full);
+            mbar_expect_tx(full + h, bytes);
+            bulk_g2s(zb + h * half, w.z + at, bytes, full + h);
         };
         // the groups' parked bests of a finished item, reduced in the
         // reference's order (better(); equal entries: the lower group, which
@@ -461,24 +467,32 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
             }
         };
         bool failed = false;
-        unsigned issued = 0, n_done = 0;
+        unsigned issued[kZfftParts] = {}, n_done = 0; // units issued per part
         if (lane == 0 && n_units > 0)
-            issue(0);
-        issued = n_units > 0 ? 1 : 0;
+            for (int h = 0; h < kZfftParts; h++)
+                issue(0, h);
+        if (n_units > 0)
+            for (int h = 0; h < kZfftParts; h++)
+                issued[h] = 1;
         for (unsigned u = 0; u < n_units; u++) {
-            // every group holds its unit-u column: the buffer takes unit u + 1
+            // every group holds its unit-u values of a part: the part takes unit u + 1
             bool ok = true;
-            if (lane == 0) {
-                ok = mbar_wait_abort(empty, u & 1u, abort_flag, wlim);
-                if (ok && u + 1 < n_units)
-                    issue(u + 1);
+#pragma unroll
+            for (int h = 0; h < kZfftParts; h++) {
+                if (lane == 0) {
+                    ok = ok && mbar_wait_abort(empty + h, u & 1u, abort_flag, wlim);
+                    if (ok && u + 1 < n_units)
+                        issue(u + 1, h);
+                }
+                if (!__shfl_sync(0xffffffffu, ok, 0))
+                    break;
+                if (u + 1 < n_units)
+                    issued[h] = u + 2;
             }
             if (!__shfl_sync(0xffffffffu, ok, 0)) {
                 failed = true;
                 break;
             }
-            if (u + 1 < n_units)
-                issued = u + 2;
             if (u % w.n_blocks == w.n_blocks - 1) {
                 const unsigned set = n_done % kZfftRing;
                 ok = mbar_wait_abort(parked + set, (n_done / kZfftRing) & 1u, abort_flag, wlim);
@@ -496,9 +510,10 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
         if (failed && lane == 0) {
             *abort_flag = 1;
             atomicExch(err, 1u);
-            // the last copy issued lands before the CTA ends (bounded)
-            if (issued && !w.test_stall)
-                mbar_wait(full, (issued - 1) & 1u, wlim);
+            // the last copies issued land before the CTA ends (bounded)
+            for (int h = 0; h < kZfftParts; h++)
+                if (issued[h] && !w.test_stall)
+                    mbar_wait(full + h, (issued[h] - 1) & 1u, wlim);
         }
         return;
     }
@@ -515,41 +530,46 @@ zfft_peak_kernel(SplitFftWork w, const float2* __restrict__ twiddle, unsigned* _
     for (unsigned u = 0; u < n_units; u++) {
         const unsigned b = u % w.n_blocks;
         const unsigned s0 = b * w.block, nsb = min(w.block, w.n_shift - s0);
-        if (!mbar_wait_abort(full, u & 1u, abort_flag, wlim)) {
-            *abort_flag = 1;
-            atomicExch(err, 1u);
-            return;
-        }
         const bool has = (unsigned)g < nsb; // group-uniform
+        // the ring sums e = (ua, va, ub, vb) of slot l + 16 m (m < 8) give
+        // Z[k] = (ua, ub) for k = l + 16 m (input m) and Z[256 - k] =
+        // (vb, va), input 15 - m of lane (16 - l) mod 16; lane 0 keeps its
+        // own: Z[256 - 16 m] is its input 16 - m, and slot 0 (the real
+        // (F[0], F[128]) products) gives Z[0] and Z[128].  Slots l + 16 m
+        // are in part m / (8 / kZfftParts) of the buffer.
         float2 x[16];
-        if (has) {
-            // the ring sums e = (ua, va, ub, vb) of slot l + 16 m (m < 8) give
-            // Z[k] = (ua, ub) for k = l + 16 m (input m) and Z[256 - k] =
-            // (vb, va), input 15 - m of lane (16 - l) mod 16; lane 0 keeps
-            // its own: Z[256 - 16 m] is its input 16 - m, and slot 0 (the
-            // real (F[0], F[128]) products) gives Z[0] and Z[128]
-            const float4* z4 = reinterpret_cast<const float4*>(zb);
-            const int partner = (16 - l) & 15;
-            float p2 = 0.f;
+        float p2 = 0.f;
+        const float4* z4 = reinterpret_cast<const float4*>(zb);
+        const int partner = (16 - l) & 15;
 #pragma unroll
-            for (int m = 0; m < 8; m++) {
-                const float4 e = z4[(l + 16 * m) * w.zw + g];
-                x[m] = make_float2(e.x, e.z);
-                x[15 - m] = make_float2(__shfl_sync(gmask, e.w, partner, 16), __shfl_sync(gmask, e.y, partner, 16));
-                if (l == 0) {
-                    if (m == 0) {
-                        const float p1 = 0.25f * (e.x + e.z + e.w + e.y);
-                        p2 = 0.25f * (e.x - e.z + e.w - e.y);
-                        x[0] = make_float2(p1, p1);
-                    } else {
-                        x[16 - m] = make_float2(e.w, e.y);
+        for (int h = 0; h < kZfftParts; h++) {
+            if (!mbar_wait_abort(full + h, u & 1u, abort_flag, wlim)) {
+                *abort_flag = 1;
+                atomicExch(err, 1u);
+                return;
+            }
+            if (has) {
+#pragma unroll
+                for (int m = h * (8 / kZfftParts); m < (h + 1) * (8 / kZfftParts); m++) {
+                    const float4 e = z4[(l + 16 * m) * w.zw + g];
+                    x[m] = make_float2(e.x, e.z);
+                    x[15 - m] =
+                        make_float2(__shfl_sync(gmask, e.w, partner, 16), __shfl_sync(gmask, e.y, partner, 16));
+                    if (l == 0) {
+                        if (m == 0) {
+                            const float p1 = 0.25f * (e.x + e.z + e.w + e.y);
+                            p2 = 0.25f * (e.x - e.z + e.w - e.y);
+                            x[0] = make_float2(p1, p1);
+                        } else {
+                            x[16 - m] = make_float2(e.w, e.y);
+                        }
                     }
                 }
             }
-            if (l == 0)
-                x[8] = make_float2(p2, p2);
+            mbar_arrive(empty + h);
         }
-        mbar_arrive(empty);
+        if (has && l == 0)
+            x[8] = make_float2(p2, p2);
         if (has)
             fft_peak_regs<true>(x, gz, tw + l * kTwRow, l, gmask, s0 + g, w.n_shift, st, w.rule);
         if (b == w.n_blocks - 1) {
@@ -592,7 +612,7 @@ static size_t mma_smem(const SplitPlan& p) { return (size_t)p.n_stages * mma_sta
 static size_t fft_smem(const SplitPlan& p)
 {
     return zfft_zbuf_bytes(p.zw) + (size_t)p.fft_groups * kPairStride * sizeof(float2) + 16 * kTwRow * sizeof(float2) +
-           kZfftRing * 64 * sizeof(PeakSlot) + (2 + 2 * kZfftRing) * sizeof(uint64_t) + 16;
+           kZfftRing * 64 * sizeof(PeakSlot) + (2 * kZfftParts + 2 * kZfftRing) * sizeof(uint64_t) + 16;
 }
 
 bool split_plan(unsigned ring_num, unsigned n_shift, unsigned n_ref, SplitPlan& p)
