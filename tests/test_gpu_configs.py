@@ -1,13 +1,14 @@
 """Parity at the workload configurations, both contractions, against the
 FP64 oracle on the same seeded inputs (gpuisac.synth):
 
-  config 0 in full   2,000 x 64^2 particles, 16 references, rings 1..29,
-                     shifts +-2 (25), mirror;
-  config 1 slice     1,000 x 76^2 particles of the 50,000-particle workload's
-                     generator against all 200 references, rings 1..35,
-                     shifts +-3 (49), SNR 0.05;
-  config 4 slice     200 x 128^2 particles against 100 of the 500
-                     references, rings 1..61, shifts +-4 (81), SNR 0.03;
+  the CPU-sized workload in full: 2,000 x 64^2 particles, 16 references,
+                     rings 1..29, shifts +-2 (25), mirror;
+  a slice of the 50,000 x 76^2 workload: 1,000 particles of its generator
+                     against all 200 references, rings 1..35, shifts +-3
+                     (49), SNR 0.05;
+  a slice of the 200,000 x 128^2 large-box workload: 200 particles against
+                     100 of the 500 references, rings 1..61, shifts +-4
+                     (81), SNR 0.03;
                      once at 256 samples per ring (the reference GPU
                      driver's ring length) and once at 512 (Numrinit's
                      maximum ring length for a last ring of 61).
@@ -16,7 +17,7 @@ Bars (floating point): every peak value within 1e-4 relative of the FP64
 oracle -- relative to max(|d|, 1% of the Cauchy-Schwarz bound L^2 sum(r+1)
 of the normalised correlation): a peak whose normalised correlation is below
 1% is a near-total cancellation, whose FP32 rounding error is set by the
-magnitudes summed (on the config-1 slice one pair of 200,000 peaks at 4.65
+magnitudes summed (on the 50,000 x 76^2 slice one pair of 200,000 peaks at 4.65
 against a bound of 4.1e7 is off by 0.47 in FP32, the reference's arithmetic
 type); the same best (reference, angle, sx, sy, mirror) on >= 99.5% of
 particles; >= 99% of all (reference, particle) tuples the same.  The
@@ -33,10 +34,10 @@ from test_gpu_align import NEAR_ZERO, compare, cs_bound
 pytestmark = pytest.mark.gpu
 
 CONFIGS = {
-    "config0_full": dict(P=2000, D=64, R=16, NR=29, rng=2, snr=0.1, radius=28.0, seed_idx=0),
-    "config1_slice": dict(P=1000, D=76, R=200, NR=35, rng=3, snr=0.05, radius=34.0, seed_idx=1),
-    "config4_slice": dict(P=200, D=128, R=100, NR=61, rng=4, snr=0.03, radius=60.0, seed_idx=4),
-    "config4_slice_l512": dict(P=200, D=128, R=100, NR=61, rng=4, snr=0.03, radius=60.0, seed_idx=4, L=512),
+    "cpu2000_full": dict(P=2000, D=64, R=16, NR=29, rng=2, snr=0.1, radius=28.0, seed_idx=0),
+    "mref76_1000x200": dict(P=1000, D=76, R=200, NR=35, rng=3, snr=0.05, radius=34.0, seed_idx=1),
+    "largebox128_200x100": dict(P=200, D=128, R=100, NR=61, rng=4, snr=0.03, radius=60.0, seed_idx=4),
+    "largebox128_200x100_l512": dict(P=200, D=128, R=100, NR=61, rng=4, snr=0.03, radius=60.0, seed_idx=4, L=512),
 }
 
 _cache = {}

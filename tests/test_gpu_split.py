@@ -29,9 +29,9 @@ def split_align(st, NR, rng, base=None):
 
 
 @pytest.mark.parametrize("P,R,D,NR,rng", [
-    (40, 12, 64, 29, 2.0),    # config-0 shape: 25 shifts, 4 K groups
-    (24, 9, 76, 35, 3.0),     # config-1 shape: 49 shifts, 5 K groups (zero group)
-    (6, 5, 128, 61, 4.0),     # config-4 shape: 81 shifts in two blocks, 8 K groups
+    (40, 12, 64, 29, 2.0),    # the 64^2 / 29-ring shape: 25 shifts, 4 K groups
+    (24, 9, 76, 35, 3.0),     # the 76^2 / 35-ring shape: 49 shifts, 5 K groups (zero group)
+    (6, 5, 128, 61, 4.0),     # the 128^2 / 61-ring shape: 81 shifts in two blocks, 8 K groups
     (5, 3, 64, 20, 5.0),      # 121 shifts in three blocks
     (1, 1, 48, 1, 0.0),       # one ring, one shift, one particle, one reference
 ])

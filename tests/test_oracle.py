@@ -55,7 +55,7 @@ def test_texture_tap_weights(oracle_mod, fx, fy):
     assert w == [256 - A - B + w11, A - w11, B - w11, w11]
 
 
-def test_reference_layout_config1(oracle_mod):
+def test_reference_layout_mref_workload(oracle_mod):
     cfg = oracle_mod.make_cfg(50000, 200, 76, 35, 256, 1.0, 3.0, 3.0)
     lay = oracle_mod.reference_layout(cfg)
     # cuFFT int32 guard: P_b * 100 * 98 * 258 <= 2^31 - 1  ->  849
