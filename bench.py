@@ -634,6 +634,87 @@ def bench_assign(args, dev, L, d_dev, cpu=True):
     return blk
 
 
+AVERAGES = {"fl": 0.2, "ff": 0.2, "sample_groups": 2}
+
+
+def bench_averages(args, dev, L, parts_d, d_dev, peak_dev, cpu=True):
+    """The averaging step after the group assignment (gpuisac_class_averages:
+    rot_shift2D of every particle by its group's pair parameters, group sums,
+    mean shifts, re-centred parameters, filt_tanl + fshift of each average)
+    on the alignment's own peaks and the assignment's groups, all in HBM, L2
+    flushed before every timed call; the host-array call; the FP64 oracle on
+    the members of sampled groups (parity and the CPU baseline)."""
+    import torch
+
+    from gpuisac.assign import assign_groups_device
+    from gpuisac.averages import class_averages, class_averages_device
+    R, P = d_dev.shape
+    D = parts_d.shape[1]
+    fl, ff = AVERAGES["fl"], AVERAGES["ff"]
+    _, bel, _ = assign_groups_device(d_dev, with_id_list=False)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)       # 256 MB > L2
+
+    def call():
+        return class_averages_device(parts_d, peak_dev, bel, fl, ff, True, stream=stream)
+
+    for _ in range(max(args.warmup, 3)):
+        out = call()
+    total = 0.0
+    steps = max(args.steps, 3)
+    launches0 = L.gpuisac_launch_count()
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out2 = call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    launches = (L.gpuisac_launch_count() - launches0) / steps
+    ms = total / steps
+    hbm_peak, _, peak_kind = peaks()
+    alg_bytes = 4.0 * P * D * D + 4.0 * R * D * D + 16.0 * P + 4.0 * P + 16.0 * P
+    avg, params, members, shifts = (t.cpu().numpy() for t in out)
+    blk = {"workload": f"{P} particles ({D}^2) x {R} groups from the assignment on this run's peaks; rot_shift2D "
+                       f"(quadratic, background), sums, mean shifts, re-centred parameters, filt_tanl({fl}, {ff}) "
+                       "and fshift by minus the mean shift",
+           "ms_per_call": ms, "particles_per_s": P / (ms / 1000.0), "kernel_launches_per_call": launches,
+           "roofline": {"bound": "issue (the interpolation: about 70 instructions per output pixel and member)",
+                        "hbm_achieved": alg_bytes / (ms / 1000.0) / 1e9, "hbm_peak": hbm_peak, "unit": "GB/s",
+                        "hbm_frac": alg_bytes / (ms / 1000.0) / 1e9 / hbm_peak, "algorithmic_bytes": alg_bytes,
+                        "peak_kind": peak_kind},
+           "repeat_identical": all(np.array_equal(a.cpu().numpy(), b.cpu().numpy()) for a, b in zip(out, out2)),
+           "l2": "256 MB buffer written before each timed call; the 1.2 GB stack exceeds L2"}
+    parts_h, pk_h, bel_h = parts_d.cpu().numpy(), peak_dev.cpu().numpy(), bel.cpu().numpy()
+    t0 = time.perf_counter()
+    class_averages(parts_h, pk_h, bel_h, fl, ff, True)
+    t_host = time.perf_counter() - t0
+    blk["e2e"] = {"ms_per_call": 1000.0 * t_host, "h2d_bytes": parts_h.nbytes + pk_h.nbytes + bel_h.nbytes,
+                  "d2h_bytes": avg.nbytes + params.nbytes + members.nbytes + shifts.nbytes,
+                  "api": "gpuisac.averages.class_averages (host arrays in and out)"}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        groups = np.unique(bel_h)[:AVERAGES["sample_groups"]]
+        idx = np.flatnonzero(np.isin(bel_h, groups))
+        remap = np.searchsorted(groups, bel_h[idx])
+        t0 = time.perf_counter()
+        a_o, p_o, m_o, s_o = oracle.class_averages(parts_h[idx], pk_h[groups][:, idx], remap, fl, ff, True)
+        t_cpu = time.perf_counter() - t0
+        err = float(np.abs(avg[groups] - a_o).max() / max(np.abs(a_o).max(), 1e-6))
+        blk["vs_fp64_oracle"] = {"groups": int(groups.size), "particles": int(idx.size),
+                                 "max_rel_average_err": err,
+                                 "max_param_err": float(np.abs(params[idx] - p_o).max()),
+                                 "members_equal": bool(np.array_equal(members[groups], m_o)),
+                                 "meets_bar": err < 2e-5 and float(np.abs(params[idx] - p_o).max()) < 2e-6}
+        blk["cpu_baseline"] = {"particles_per_s": idx.size / t_cpu, "cores": 1, "kind": "port",
+                               "sample": f"the {idx.size} members of {groups.size} groups, FP64 numpy restatement, "
+                                         f"{t_cpu:.1f} s"}
+    del flush
+    return blk
+
+
 MULTIGROUP = {"workload": "stability-test multigroup alignment: the 50,000 particles (76^2) sorted into classes of "
                           "at most 100 (each true class split into runs), 35 rings, shift range 1 (9 shifts), "
                           "30 iterations with the tangent filter ramp 0.1 -> 0.3, fall-off 0.2 (ISAC's defaults "
@@ -1138,6 +1219,9 @@ def bench_ours(args):
         big[cls, torch.arange(100000, device=dev)] += 0.3 * torch.rand(100000, generator=rng, device=dev)
         assign_blk["synthetic_100000x500"] = bench_assign(args, dev, L, big, cpu=False)
         del big
+    averages_blk = None
+    if rank == 0 and world == 1 and not args.no_averages:
+        averages_blk = bench_averages(args, dev, L, parts_d, d_out, peak_out, cpu=not args.no_cpu)
     multigroup_blk = prealign_blk = None
     if rank == 0 and world == 1 and not args.no_multigroup and WORKLOAD["workload"].startswith("mref"):
         multigroup_blk = bench_multigroup(args, dev, L, st)
@@ -1180,7 +1264,8 @@ def bench_ours(args):
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "split_kernels": split_ms if args.contraction == "bf16x3" else None,
                 "precision_vs_fp64": prec, "grouped": grouped_blk, "learned": learned_blk,
-                "assign_groups": assign_blk, "multigroup": multigroup_blk, "prealign": prealign_blk}
+                "assign_groups": assign_blk, "averages": averages_blk, "multigroup": multigroup_blk,
+                "prealign": prealign_blk}
         print(json.dumps(line), flush=True)
         if prec is not None and not prec["meets_bar"]:
             sys.stderr.write("precision_vs_fp64: the parity bar is not met\n")
@@ -1212,6 +1297,7 @@ def main():
     ap.add_argument("--no-learned-as-written", action="store_true",
                     help="skip the learned proposal as the workload writes it (64 harmonics, top-8)")
     ap.add_argument("--no-assign", action="store_true", help="skip the group-assignment block")
+    ap.add_argument("--no-averages", action="store_true", help="skip the averaging-step block")
     ap.add_argument("--no-multigroup", action="store_true", help="skip the multigroup (stability test) block")
     ap.add_argument("--no-prealign", action="store_true", help="skip the pre-alignment block")
     ap.add_argument("--no-autotune", action="store_true", help="default tile shape (profiling runs)")

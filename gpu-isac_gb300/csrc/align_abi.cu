@@ -1104,7 +1104,7 @@ int gpuisac_checked_failures(unsigned long long* first)
 {
 #ifdef GPUISAC_CHECKED
     void (*readers[])(unsigned&, unsigned long long&) = {checked_read_spectra, checked_read_split, checked_read_ccf,
-                                                         checked_read_ring512};
+                                                         checked_read_ring512, checked_read_averages};
     unsigned total = 0;
     unsigned long long f = 0;
     for (auto rd : readers) {

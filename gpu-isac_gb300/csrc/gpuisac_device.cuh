@@ -49,7 +49,7 @@ __device__ __forceinline__ bool chk_in_bounds(unsigned site, unsigned long long 
 // guarded sites (the high 16 bits of a recorded failure)
 enum {
     kChkSpectraOut = 1, kChkSpectraTmpl, kChkOperandOut, kChkMmaZ, kChkMmaA, kChkMmaB, kChkZfftZ, kChkZfftOut,
-    kChkMergeOut, kChkCcfRow, kChkR512Out, kChkR512Row, kChkR512Res
+    kChkMergeOut, kChkCcfRow, kChkR512Out, kChkR512Row, kChkR512Res, kChkAvgImg, kChkAvgPartial, kChkAvgOut
 };
 
 constexpr int kRingLen = 256;        // polar samples per ring (angles)

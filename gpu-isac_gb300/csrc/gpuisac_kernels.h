@@ -300,5 +300,6 @@ void checked_read_spectra(unsigned& count, unsigned long long& first);
 void checked_read_split(unsigned& count, unsigned long long& first);
 void checked_read_ccf(unsigned& count, unsigned long long& first);
 void checked_read_ring512(unsigned& count, unsigned long long& first);
+void checked_read_averages(unsigned& count, unsigned long long& first);
 
 } // namespace gpuisac

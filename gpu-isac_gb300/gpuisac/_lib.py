@@ -50,7 +50,7 @@ EXPORTS = (
     "gpuisac_nn_affine_cols", "gpuisac_nn_group_max", "gpuisac_learned_align_device", "gpuisac_autotune_ccf",
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
     "gpuisac_ref_free_averages", "gpuisac_set_contraction", "gpuisac_get_contraction", "gpuisac_test_stall_ccf", "gpuisac_normalize_mask",
-    "gpuisac_split_plan", "gpuisac_groups_stats", "gpuisac_checked_failures",
+    "gpuisac_split_plan", "gpuisac_groups_stats", "gpuisac_checked_failures", "gpuisac_class_averages",
 )
 
 
@@ -201,6 +201,11 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_normalize_mask.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p]
     L.gpuisac_normalize_mask.restype = ctypes.c_int
+    L.gpuisac_class_averages.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p,
+                                         ctypes.c_ulonglong, ctypes.c_void_p, ctypes.c_uint, ctypes.c_float,
+                                         ctypes.c_float, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.gpuisac_class_averages.restype = ctypes.c_int
     L.gpuisac_split_plan.argtypes = [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint),
                                      ctypes.c_uint]
     L.gpuisac_split_plan.restype = ctypes.c_int

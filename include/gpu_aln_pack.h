@@ -141,6 +141,35 @@ int gpuisac_ref_free_averages(float *out);
 int gpuisac_normalize_mask(float *imgs, unsigned int n_img, unsigned int img_dim, const float *mask, int no_sigma,
                            void *stream);
 
+/* Replaces the averaging step that follows the group assignment in every
+ * ISAC main iteration (bin/sp_isac2_gpu.py:1153-1234, the peak conversion
+ * before it at :1015-1022; the image operations are EMAN2's, not part of the
+ * reference tree).  Device arrays:
+ *   imgs [n_img][img_dim][img_dim] the particles as they were aligned;
+ *   peaks [n_class][peak_pitch][4] the alignment's (angle, sx, sy, mirror) per
+ *     (reference, particle), as gpuisac_multi_ref_align_device writes them
+ *     (peak_pitch 0 = n_img; 16-byte aligned);
+ *   belongsto [n_img] each particle's group (gpuisac_assign_groups_device).
+ * Particle i of group r takes the caller's conversion of peaks[r][i]
+ * (sx' = -sx cos a - sy sin a, sy' = sx sin a - sy cos a, as float); its image
+ * rot_shift2D'd by (a, sx', sy', mirror) -- quadratic interpolation,
+ * "background" mode, the x-mirror after -- is added to the group's sum.  Each
+ * group's mean shift (sx' negated for mirrored particles, summed in FP64,
+ * rounded to float, divided by the member count) re-centres its members:
+ * params[i] = (a, sx' -/+ mean x, sy' - mean y, mirror), the values the caller
+ * stores with set_params2D.  averages[r] = sum times float(1 / members),
+ * filt_tanl(fl, ff) when fl > 0 (0 <= ff <= 0.5, fl <= 0.5 in cycles per
+ * pixel), then fshift by minus the mean shift when center.  members [n_class]
+ * and shifts [n_class][2] (the mean shifts) are optional outputs, as is params.
+ * img_dim 2..256.  Blocks until done.  Returns 0; 2 for bad arguments, a
+ * belongsto entry outside [0, n_class) or a group without members (the
+ * caller's division by the member count fails there; its average is zero); 1
+ * for a CUDA error. */
+int gpuisac_class_averages(const float *imgs, unsigned int n_img, unsigned int img_dim, const float *peaks,
+                           unsigned long long peak_pitch, const int *belongsto, unsigned int n_class, float fl,
+                           float ff, int center, float *averages, float *params, int *members, float *shifts,
+                           void *stream);
+
 /* ---- additions of this library (no counterpart in the reference, which
  * prints and exits on any CUDA error, cuda/gpu_aln_common.cu:104-118) ---- */
 

@@ -372,3 +372,144 @@ def ormq_post(peak, base=None):
     sxn, syn = -peak[..., 1], -peak[..., 2]
     c, s = np.cos(np.radians(ang)), -np.sin(np.radians(ang))
     return ang, sxn * c - syn * s, sxn * s + syn * c, peak[..., 3]
+
+
+def quadri(img, xo, yo) -> np.ndarray:
+    """Quadratic interpolation of one image [D][D] at 0-based coordinates
+    (xo, yo) in [0, D), neighbours taken periodically: the six-point scheme of
+    SPIDER's QUADRI as EMAN2's Util::quadri implements it (the interpolation
+    that rot_shift2D uses by default), restated from its published definition
+    in FP64.  With f00 at (i, j) = floor, dx, dy the fractions:
+    f = f00 + dx (c1 + (dx - 1) c2 + dy c5) + dy (c3 + (dy - 1) c4), c1, c3
+    the forward differences along x, y, c2, c4 half the second differences,
+    c5 the cross term through (i + 1, j + 1).  Exact for every quadratic
+    a + bx + cx^2 + dy + ey^2 + gxy away from the wrap."""
+    f = np.asarray(img, np.float64)
+    D = f.shape[0]
+    xo = np.asarray(xo, np.float64)
+    yo = np.asarray(yo, np.float64)
+    i = np.floor(xo).astype(np.int64)
+    j = np.floor(yo).astype(np.int64)
+    dx, dy = xo - i, yo - j
+    i %= D
+    j %= D
+    ip, im, jp, jm = (i + 1) % D, (i - 1) % D, (j + 1) % D, (j - 1) % D
+    f00 = f[j, i]
+    c1 = f[j, ip] - f00
+    c2 = (c1 - f00 + f[j, im]) * 0.5
+    c3 = f[jp, i] - f00
+    c4 = (c3 - f00 + f[jm, i]) * 0.5
+    c5 = f[jp, ip] - f00 - c1 - c3
+    return f00 + dx * (c1 + (dx - 1.0) * c2 + dy * c5) + dy * (c3 + (dy - 1.0) * c4)
+
+
+def rot_shift2d_coords(D: int, c, s, sx, sy, mirror):
+    """Source coordinates (xo, yo) [D][D] (float32) that rot_shift2D(img, ang,
+    sx, sy, mirror) samples for each output pixel, as EMAN2's
+    rot_scale_trans2D_background (the default "background" mode) and the
+    x-mirror after it define them: output column ix comes from the rotation's
+    column ixs = (D - ix) mod D when mirrored (the mirror about column D/2
+    keeps column 0), x = ixs - (D/2 + sx), y = iy - (D/2 + sy) and
+    xo = (x c - y s) + D/2, yo = (x s + y c) + D/2 with c = cos(ang),
+    s = sin(ang); a source point outside [0, D)^2 is replaced by the pixel
+    (ixs, iy) itself.  Every step is one float32 operation in this order; the
+    GPU kernel rounds the same operations."""
+    f32 = np.float32
+    h = f32(D // 2)
+    c, s = f32(c), f32(s)
+    iy, ix = np.meshgrid(np.arange(D), np.arange(D), indexing="ij")
+    ixs = (D - ix) % D if mirror else ix
+    x = ixs.astype(f32) - (h + f32(sx))
+    y = iy.astype(f32) - (h + f32(sy))
+    xo = (x * c - y * s) + h
+    yo = (x * s + y * c) + h
+    out = (xo < 0) | (xo >= f32(D)) | (yo < 0) | (yo >= f32(D))
+    return np.where(out, ixs.astype(f32), xo), np.where(out, iy.astype(f32), yo)
+
+
+def rot_shift2d(img, ang, sx, sy, mirror) -> np.ndarray:
+    """rot_shift2D(img, ang, sx, sy, mirror) with quadratic interpolation,
+    background mode (FP64 values, float32 coordinates): rotate by ang degrees
+    about (D/2, D/2), shift by (sx, sy), then mirror in x.  cos and sin of the
+    angle in FP64, rounded to float32."""
+    D = np.asarray(img).shape[0]
+    t = np.radians(np.float64(ang))
+    xo, yo = rot_shift2d_coords(D, np.cos(t), np.sin(t), sx, sy, int(mirror))
+    return quadri(img, xo, yo)
+
+
+def tanl_fshift(img, fl: float, ff: float, dx: float, dy: float) -> np.ndarray:
+    """filt_tanl(img, fl, ff) followed by fshift(img, dx, dy) on one image
+    [D][D], both on its real FFT in FP64 (numpy's rfft2 / irfft2): the
+    half spectrum times 0.5 (tanh(k (r + fl)) - tanh(k (r - fl))),
+    k = pi / (2 ff fl), r = |(kx, ky)| / D in cycles per pixel (ky signed,
+    ky > D/2 taken as ky - D),
+    no filter when fl <= 0, a step at fl when ff = 0; times
+    exp(-2 pi i (kx dx + ky dy) / D), the image moved by (+dx, +dy)."""
+    a = np.asarray(img, np.float64)
+    D = a.shape[0]
+    kx = np.arange(D // 2 + 1, dtype=np.float64)
+    ky = np.arange(D, dtype=np.float64)
+    ky[ky > D // 2] -= D  # ky = D/2 (even D) counts as +D/2
+    h = np.ones((D, D // 2 + 1))
+    if fl > 0:
+        r = np.sqrt((kx[None, :] / D) ** 2 + (ky[:, None] / D) ** 2)
+        if ff > 0:
+            k = np.pi / (2.0 * ff * fl)
+            h = 0.5 * (np.tanh(k * (r + fl)) - np.tanh(k * (r - fl)))
+        else:  # the limit ff -> 0: a step at fl
+            h = np.where(r < fl, 1.0, np.where(r == fl, 0.5, 0.0))
+    ph = np.exp(-2j * np.pi * (kx[None, :] * dx + ky[:, None] * dy) / D)
+    return np.fft.irfft2(np.fft.rfft2(a) * h * ph, s=(D, D))
+
+
+def class_averages(imgs, peaks, belongsto, fl: float, ff: float, center: bool = True):
+    """The averaging step after the group assignment
+    (bin/sp_isac2_gpu.py:1153-1234), restated in FP64 for one process:
+    each particle i of group r = belongsto[i] takes the alignment parameters
+    of its pair (peaks[r][i], converted as the caller does, ormq_post; stored
+    as float32 like the caller's peak_list); its image rot_shift2D'd by them
+    is added to the group's sum; the group's shift sums (sx subtracted for a
+    mirrored particle) are summed in FP64 in particle order, rounded to
+    float32 (the MPI_FLOAT reduction) and divided by the member count; every
+    particle's parameters become (ang, sx -/+ mean sx, sy - mean sy, mirror);
+    each sum times float32(1 / members) is low-passed (filt_tanl(fl, ff)) and
+    moved by minus its mean shift (fshift), when center.
+    Returns (averages [R][D][D] FP64, params [P][4] FP64 rounded to float32,
+    members [R], shifts [R][2])."""
+    imgs = np.asarray(imgs, np.float32)
+    P, D = imgs.shape[0], imgs.shape[1]
+    pk = np.asarray(peaks, np.float32)
+    R = pk.shape[0]
+    bel = np.asarray(belongsto, np.int64)
+    f32 = np.float32
+    ang, sxc, syc, mir = ormq_post(pk[bel, np.arange(P)])
+    ang = ang.astype(f32)
+    sxc, syc = sxc.astype(f32), syc.astype(f32)
+    mir = mir.astype(np.int64)
+    sums = np.zeros((R, D, D))
+    members = np.zeros(R, np.int64)
+    ssx, ssy = np.zeros(R), np.zeros(R)
+    for i in range(P):
+        r = bel[i]
+        sums[r] += rot_shift2d(imgs[i], ang[i], sxc[i], syc[i], mir[i])
+        members[r] += 1
+        ssx[r] += -float(sxc[i]) if mir[i] else float(sxc[i])
+        ssy[r] += float(syc[i])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        mx = np.where(members > 0, ssx.astype(f32).astype(np.float64) / members, 0.0)
+        my = np.where(members > 0, ssy.astype(f32).astype(np.float64) / members, 0.0)
+    params = np.zeros((P, 4))
+    params[:, 0] = ang
+    params[:, 1] = np.where(mir == 0, sxc - mx[bel], sxc + mx[bel]).astype(f32)
+    params[:, 2] = (syc - my[bel]).astype(f32)
+    params[:, 3] = mir
+    avg = np.zeros((R, D, D))
+    for r in range(R):
+        if members[r] == 0:
+            continue
+        a = sums[r] * np.float64(f32(1.0 / members[r]))
+        if fl > 0 or center:
+            a = tanl_fshift(a, fl, ff, -mx[r] if center else 0.0, -my[r] if center else 0.0)
+        avg[r] = a
+    return avg, params, members, np.stack([mx, my], 1)

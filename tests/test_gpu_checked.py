@@ -1,11 +1,11 @@
 """The bounds-checked build (gpu-isac_gb300/build.py --checked, -DGPUISAC_CHECKED)
 on small cases of every alignment path -- FP32 and tensor-core contractions
 at 76^2 / 35 rings and 128^2 / 61 rings (two shift blocks), 512-sample rings,
-the grouped launch sequence -- run in a child process that loads the checked
-library (GPUISAC_LIBRARY).  Every guarded access of the spectra, operand,
-contraction, FFT and peak kernels must stay inside the extent its kernel was
-given (no access skipped), and every result must equal the normal build's bit
-for bit."""
+the grouped launch sequence, the averaging step at four image sides -- run in
+a child process that loads the checked library (GPUISAC_LIBRARY).  Every
+guarded access of the spectra, operand, contraction, FFT, peak and averaging
+kernels must stay inside the extent its kernel was given (no access skipped),
+and every result must equal the normal build's bit for bit."""
 import os
 import subprocess
 import sys
@@ -41,6 +41,14 @@ dev = torch.device("cuda:0")
 parts, refs = torch.from_numpy(st.particles).to(dev), torch.from_numpy(st.refs).to(dev)
 dg, pg, _ = multi_ref_align_groups_device(parts, refs, [(0, 25, 0, 3), (25, 35, 2, 5), (5, 1, 6, 1)], 35, 3.0, 3.0)
 out["groups_d"], out["groups_p"] = dg.cpu().numpy(), pg.cpu().numpy()
+from gpuisac.averages import class_averages
+rng = np.random.default_rng(3)
+for D in (64, 65, 150, 200):
+    imgs = rng.standard_normal((90, D, D)).astype(np.float32)
+    pk = np.concatenate([rng.uniform(0, 360, (3, 90, 1)), rng.uniform(-3, 3, (3, 90, 2)),
+                         rng.integers(0, 2, (3, 90, 1))], 2).astype(np.float32)
+    avg, prm, mem, sh = class_averages(imgs, pk, np.arange(90) % 3, 0.2, 0.2, True)
+    out[f"avg{D}"], out[f"avg{D}_p"] = avg, prm
 first = ctypes.c_ulonglong()
 out["failures"] = np.array([L.gpuisac_checked_failures(ctypes.byref(first)), first.value], np.int64)
 np.savez(sys.argv[2], **out)
