@@ -680,7 +680,7 @@ def bench_averages(args, dev, L, parts_d, d_dev, peak_dev, cpu=True):
                        f"(quadratic, background), sums, mean shifts, re-centred parameters, filt_tanl({fl}, {ff}) "
                        "and fshift by minus the mean shift",
            "ms_per_call": ms, "particles_per_s": P / (ms / 1000.0), "kernel_launches_per_call": launches,
-           "roofline": {"bound": "issue (the interpolation: about 70 instructions per output pixel and member)",
+           "roofline": {"bound": "issue (the interpolation: about 80 instructions per output pixel and member)",
                         "hbm_achieved": alg_bytes / (ms / 1000.0) / 1e9, "hbm_peak": hbm_peak, "unit": "GB/s",
                         "hbm_frac": alg_bytes / (ms / 1000.0) / 1e9 / hbm_peak, "algorithmic_bytes": alg_bytes,
                         "peak_kind": peak_kind},
