@@ -5,8 +5,10 @@ same float operations; the conversion and mean shifts are FP64 on both
 sides), member counts and mean shifts equal.  Image sides cover the staged
 path (even sides up to 160, bulk copies of whole images), odd sides and the
 larger sides read from global memory, two passes of output rows (sides above
-128) and the finish kernel's spectra in global memory (sides above 160).
-Also: more than 1024 groups (the group scan's carry), the chain with the
+128), the finish kernel's spectra in global memory (sides above 160) and
+sides of 4 and 5 pixels (every neighbour next to the wrap).  Also: more than
+1,024 groups (the group scan's carry) and more than 16,384 (the scatter's
+running counts in global memory), the chain with the
 alignment and the group assignment on one stream, the errors the reference's
 caller would meet (a group without members, a group index out of range), and
 repeat calls bit-identical."""
@@ -64,11 +66,41 @@ def test_averages_match_oracle(gpulib, cuda, oracle_mod, P, R, D, fl, ff, center
     print(f"P={P} R={R} D={D}: max |avg - oracle| / max |avg| = {err:.2e}")
 
 
-def test_many_groups(gpulib, cuda, oracle_mod):
+@pytest.mark.parametrize("P,R,D", [
+    (4000, 1500, 16),    # the group scan's carry over 1,024-group tiles
+    (300, 7, 4),         # every source point next to the periodic wrap
+    (200, 5, 5),
+])
+def test_many_groups_and_tiny_images(gpulib, cuda, oracle_mod, P, R, D):
     from gpuisac.averages import class_averages
-    imgs, peaks, bel = _case(4000, 1500, 16, 9)
+    imgs, peaks, bel = _case(P, R, D, 9 + D)
     out = class_averages(imgs, peaks, bel, 0.2, 0.2, True)
     _compare(oracle_mod, imgs, peaks, bel, 0.2, 0.2, True, out)
+
+
+def test_more_groups_than_shared_memory_counts(gpulib, cuda, oracle_mod):
+    """16,400 groups: the scatter keeps each chunk's running counts in global
+    memory.  Every group's peak row holds the same per-particle parameters
+    (the matrix is 4.3 GB on the device; the oracle reads a strided view)."""
+    import torch
+
+    from gpuisac.averages import class_averages_device
+    P, R, D = 16500, 16400, 4
+    rng = np.random.default_rng(77)
+    imgs = rng.standard_normal((P, D, D)).astype(np.float32)
+    row = np.zeros((1, P, 4), np.float32)
+    row[..., 0] = rng.uniform(0.0, 360.0, P)
+    row[..., 1:3] = rng.uniform(-2.0, 2.0, (P, 2))
+    row[..., 3] = rng.uniform(size=P) < 0.5
+    bel = rng.integers(0, R, P).astype(np.int32)
+    bel[:R] = rng.permutation(R)
+    peaks_d = torch.from_numpy(row).to(cuda).expand(R, P, 4).contiguous()
+    out = class_averages_device(torch.from_numpy(imgs).to(cuda), peaks_d, torch.from_numpy(bel).to(cuda),
+                                0.2, 0.2, True)
+    del peaks_d
+    out = tuple(t.cpu().numpy() for t in out)
+    view = np.lib.stride_tricks.as_strided(row, shape=(R, P, 4), strides=(0,) + row.strides[1:])
+    _compare(oracle_mod, imgs, view, bel, 0.2, 0.2, True, out)
 
 
 def test_repeat_calls_identical(gpulib, cuda):
