@@ -292,6 +292,7 @@ struct AvgSumArgs {
     float* partial;
     unsigned* err;
     unsigned P, R, D, G, piece;
+    unsigned test_stall, wait_iters; // failure-path tests only (gpuisac_test_stall_ccf)
 };
 
 // The interpolated value of output pixel (ixs, iy) of one member: the source
@@ -369,7 +370,10 @@ avg_sum_kernel(AvgSumArgs a)
     const unsigned tid = threadIdx.x, ix = tid % D, g = tid / D;
     const size_t npix = (size_t)D * D;
     const uint32_t bytes = (uint32_t)(npix * sizeof(float));
+    const uint32_t wlim = wait_tries(a.wait_iters);
     auto issue = [&](unsigned k, unsigned buf) {
+        if (a.test_stall)
+            return; // failure-path test: no copy, a wait that runs out
         const AvgMember b = a.rec[a.order[k]];
         if (GPUISAC_IN_BOUNDS(kChkAvgImg, b.img, a.P)) {
             mbar_expect_tx(&bars[buf], bytes);
@@ -401,17 +405,17 @@ avg_sum_kernel(AvgSumArgs a)
             }
             for (unsigned k = k0; k < k1; k++, u++) {
                 const unsigned buf = u & 1u;
-                const bool ok = mbar_wait(&bars[buf], (u >> 1) & 1u);
+                const bool ok = mbar_wait(&bars[buf], (u >> 1) & 1u, wlim);
                 if (ok)
                     accumulate(acc, sbuf + buf * npix, a.rec[a.order[k]], ix, row0 + g, G, D);
                 if (__syncthreads_or(!ok)) {
                     if (tid == 0) {
                         atomicAdd(a.err + kErrWait, 1u);
                         // the copies still in flight land before the CTA leaves
-                        if (!ok)
-                            mbar_wait(&bars[buf], (u >> 1) & 1u);
-                        if (k + 1 < k1)
-                            mbar_wait(&bars[buf ^ 1u], ((u + 1) >> 1) & 1u);
+                        if (!ok && !a.test_stall)
+                            mbar_wait(&bars[buf], (u >> 1) & 1u, wlim);
+                        if (k + 1 < k1 && !a.test_stall)
+                            mbar_wait(&bars[buf ^ 1u], ((u + 1) >> 1) & 1u, wlim);
                     }
                     return;
                 }
@@ -794,7 +798,9 @@ extern "C" int gpuisac_class_averages(const float* imgs, unsigned int n_img, uns
     avg_scatter_kernel<<<n_chunks, 32, scat_smem, st>>>(belongsto, P, R, w.cnt.p, w.start.p, w.order.p);
     avg_shift_kernel<<<(R + 7) / 8, 256, 0, st>>>(w.rec.p, w.order.p, w.start.p, w.total.p, R, w.mean.p,
                                                   reinterpret_cast<float2*>(shifts), reinterpret_cast<float4*>(params));
-    AvgSumArgs sa{imgs, w.rec.p, w.order.p, w.start.p, w.total.p, w.pstart.p, w.partial.p, w.err.p, P, R, D, G, piece};
+    AvgSumArgs sa{imgs, w.rec.p, w.order.p, w.start.p, w.total.p, w.pstart.p, w.partial.p, w.err.p, P, R, D, G, piece,
+                  0, 0};
+    ccf_test_settings(sa.test_stall, sa.wait_iters);
     sum_kernel<<<(unsigned)pieces_cap, sum_threads, sum_smem, st>>>(sa);
     AvgFinishArgs fa{w.partial.p, w.pstart.p, w.total.p, w.mean.p, w.tw.p, fin_smem ? nullptr : w.scratch.p,
                      averages, R, D, fl, ff, center};
@@ -813,7 +819,7 @@ extern "C" int gpuisac_class_averages(const float* imgs, unsigned int n_img, uns
         return fail(2, msg);
     }
     if (w.h_err[kErrWait])
-        return fail(1, "class_averages: an image copy did not complete (bounded wait ran out)");
+        return fail(1, "class_averages: an image copy timed out (bounded wait ran out)");
     if (w.h_err[kErrEmpty]) {
         snprintf(msg, sizeof(msg), "class_averages: %u groups have no members, the first is group %u",
                  w.h_err[kErrEmpty], w.h_err[kErrEmptyFirst]);

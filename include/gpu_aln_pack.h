@@ -207,11 +207,11 @@ int gpuisac_multi_ref_align_device(const AlignConfig *cfg, const float *sbj, con
  * unknown one. */
 /* No counterpart in the reference (whose CUDA errors exit the process).  For
  * failure-path tests only: while wait_iters > 0, the kernels that stage their
- * inputs with asynchronous bulk copies (the tensor-memory CCF kernels and both
- * kernels of the tensor-core contraction) issue no copies and give up each
- * bounded wait after wait_iters tries of at most 20 us, so that an alignment
- * call comes back with error code 1 ("timed out") and the context stays
- * usable; 0 restores normal operation. */
+ * inputs with asynchronous bulk copies (the tensor-memory CCF kernels, both
+ * kernels of the tensor-core contraction and the averaging step's sum kernel)
+ * issue no copies and give up each bounded wait after wait_iters tries of at
+ * most 20 us, so that the call comes back with error code 1 ("timed out") and
+ * the context stays usable; 0 restores normal operation. */
 void gpuisac_test_stall_ccf(unsigned int wait_iters);
 
 #define GPUISAC_CONTRACTION_FP32 0

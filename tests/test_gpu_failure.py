@@ -46,3 +46,29 @@ def test_stalled_wait_returns_error_and_context_survives(gpulib, cuda, oracle_mo
     pl, d = multi_ref_align(stack.particles, stack.refs, 29, 2.0, 2.0, contraction_mode=mode)
     peak_o, d_o = oracle_run(oracle_mod, stack.particles, stack.refs, 29, 2.0, tex=gpulib.get_texture_limit(64))
     compare(pl.reshape(6, 24, 4), d, peak_o, d_o)
+
+
+def test_stalled_averaging_wait_returns_error_and_context_survives(gpulib, cuda, oracle_mod):
+    """The averaging step's sum kernel stages each member image with a bulk
+    copy: stalled, the call reports the timeout and the next call is right."""
+    from gpuisac.averages import class_averages
+    rng = np.random.default_rng(5)
+    P, R, D = 400, 5, 64
+    imgs = rng.standard_normal((P, D, D)).astype(np.float32)
+    peaks = np.concatenate([rng.uniform(0, 360, (R, P, 1)), rng.uniform(-3, 3, (R, P, 2)),
+                            rng.integers(0, 2, (R, P, 1))], 2).astype(np.float32)
+    bel = (np.arange(P) % R).astype(np.int32)
+    gpulib.gpuisac_clear_error()
+    gpulib.gpuisac_test_stall_ccf(64)
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(GpuIsacError, match="timed out"):
+            class_averages(imgs, peaks, bel, 0.2, 0.2, True)
+        assert time.perf_counter() - t0 < 30.0
+    finally:
+        gpulib.gpuisac_test_stall_ccf(0)
+        gpulib.gpuisac_clear_error()
+    avg, prm, mem, sh = class_averages(imgs, peaks, bel, 0.2, 0.2, True)
+    a_o, p_o, m_o, s_o = oracle_mod.class_averages(imgs, peaks, bel, 0.2, 0.2, True)
+    assert np.abs(avg - a_o).max() < 2e-5 * np.abs(a_o).max()
+    assert np.abs(prm - p_o).max() < 2e-6
