@@ -116,3 +116,18 @@ def test_class_averages_centre_moves_average(oracle_mod):
     assert np.allclose(sh[0], [2.0, 0.0])
     assert np.abs(a1[0] - np.roll(a0[0], -2, axis=1)).max() < 1e-9
     assert np.allclose(prm[:, 1], 0.0)
+
+
+def test_base_shifts_invert_the_caller_conversion(oracle_mod):
+    """gpuisac.isac.base_shifts_of gives back the alignment's shift from the
+    parameters the caller's conversion made of it, at any angle."""
+    from gpuisac.isac import base_shifts_of
+    rng = np.random.default_rng(12)
+    n = 1000
+    peak = np.zeros((n, 4))
+    peak[:, 0] = rng.uniform(0.0, 360.0, n)
+    peak[:, 1:3] = rng.uniform(-6.0, 6.0, (n, 2))
+    peak[:, 3] = rng.integers(0, 2, n)
+    ang, sxs, sys_, mir = oracle_mod.ormq_post(peak)
+    back = base_shifts_of(np.stack([ang, sxs, sys_, mir], 1))
+    assert np.abs(back - peak[:, 1:3]).max() < 1e-5
