@@ -184,6 +184,8 @@ unsigned texture_image_limit(int dev, unsigned dim)
 }
 
 // ---------------------------------------------------------------- device buffers
+std::atomic<unsigned> g_fail_allocs{0};
+
 template <typename T>
 struct DevBuf {
     T* p = nullptr;
@@ -196,6 +198,11 @@ struct DevBuf {
             cudaFree(p);
         p = nullptr;
         n = 0;
+        if (take_injected_alloc_failure()) {
+            set_error(E_NOMEM, "cudaMalloc of %zu bytes failed: injected (gpuisac_test_fail_alloc)",
+                      count * sizeof(T));
+            return E_NOMEM;
+        }
         cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
         if (e != cudaSuccess) {
             set_error(E_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
@@ -506,6 +513,7 @@ int run_alignment_split(const Geometry& g, Workspace& ws, const StackDesc& refs,
     }
     unsigned prev_p0 = 0, prev_n = 0, slot = 0, c = 0;
     for (unsigned p0 = 0; p0 < g.P; p0 += (unsigned)chunk, c++) {
+        const NvtxRange chunk_range("gpuisac:particle_chunk");
         const unsigned n = (unsigned)std::min<size_t>(chunk, g.P - p0);
         const unsigned buf = c & 1u;
         unsigned char* const sop = ws.sop.p + buf * sop_bytes;
@@ -845,6 +853,14 @@ void record_error(int code, const char* msg) { set_error(code, "%s", msg); }
 
 std::vector<float2> shift_grid_of(float rx, float ry, float step) { return shift_grid(rx, ry, step); }
 
+bool take_injected_alloc_failure()
+{
+    unsigned k = g_fail_allocs.load();
+    while (k && !g_fail_allocs.compare_exchange_weak(k, k - 1)) {
+    }
+    return k != 0;
+}
+
 } // namespace gpuisac
 
 // ====================================================================== C-ABI
@@ -900,6 +916,7 @@ AlignParam* multi_ref_align_init(const AlignConfig* aln_cfg, unsigned int cuda_d
 void multi_ref_align(const float** sbj_data, const float** ref_data, float* isac_peak_list, float* isac_d,
                      unsigned int isac_d_pitch, float cuda_mem_request)
 {
+    const NvtxRange range("gpuisac:multi_ref_align");
     std::lock_guard<std::mutex> lk(g_api_mu);
     State& s = g_state;
     // the configuration may have been edited between init and this call
@@ -994,6 +1011,7 @@ int gpuisac_shift_count(const AlignConfig* cfg)
 int gpuisac_multi_ref_align_device(const AlignConfig* cfg, const float* sbj, const float* ref,
                                    const float* base_shift, float* d_out, float* peak_out, void* stream)
 {
+    const NvtxRange range("gpuisac:multi_ref_align_device");
     Geometry g;
     int rc = validate(cfg, g, false, true);
     if (rc)
@@ -1099,6 +1117,8 @@ int gpuisac_ccf_peak_device(const AlignConfig* cfg, const float* sbj_spectra, co
 }
 
 unsigned long long gpuisac_launch_count(void) { return g_kernel_launches.load(); }
+
+void gpuisac_test_fail_alloc(unsigned int n) { g_fail_allocs.store(n); }
 
 int gpuisac_checked_failures(unsigned long long* first)
 {

@@ -602,6 +602,7 @@ extern "C" int gpuisac_assign_groups_device(const float* d, unsigned long long d
                                             unsigned int nima, int* belongsto, int* id_list_long,
                                             unsigned int* rounds, void* stream)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:assign_groups");
     if (d_pitch == 0)
         d_pitch = nima;
     int rc = check_args(d, d_pitch, nref, nima);

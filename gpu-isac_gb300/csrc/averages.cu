@@ -715,6 +715,7 @@ extern "C" int gpuisac_class_averages(const float* imgs, unsigned int n_img, uns
                                       float fl, float ff, int center, float* averages, float* params, int* members,
                                       float* shifts, void* stream_)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:class_averages");
     if (!imgs || !peaks || !belongsto || !averages)
         return fail(2, "class_averages: NULL imgs, peaks, belongsto or averages");
     if (n_img == 0 || n_class == 0)

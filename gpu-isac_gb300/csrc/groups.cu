@@ -177,6 +177,7 @@ extern "C" int gpuisac_multi_ref_align_groups_device(const AlignConfig* cfg, con
                                                      const float* base_shift, float* d_out, float* peak_out,
                                                      void* stream)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:multi_ref_align_groups");
     const auto t_call = std::chrono::steady_clock::now();
     HostGeometry geo;
     int rc = host_geometry(cfg, geo);

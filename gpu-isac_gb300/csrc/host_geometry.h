@@ -3,12 +3,27 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <vector>
 
 #include "../../include/gpu_aln_pack.h"
 
 namespace gpuisac {
+
+// A named NVTX range for the lifetime of the object: the entry points and the
+// particle chunks of the pipeline show up by name in a timeline or an
+// ncu --nvtx capture (header-only NVTX; no cost without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+// failure-path tests (gpuisac_test_fail_alloc): true while injected failures
+// of workspace allocations are pending; each call consumes one
+bool take_injected_alloc_failure();
 
 struct HostGeometry {
     unsigned P = 0, R = 0, D = 0, NR = 0, S = 0;

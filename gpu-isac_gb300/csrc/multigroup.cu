@@ -612,6 +612,7 @@ AlignParam* ref_free_alignment_2D_init(const AlignConfig* aln_cfg, const float**
 
 void ref_free_alignment_2D(void)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:ref_free_alignment_2D");
     std::lock_guard<std::mutex> lk(g_mg.mu);
     if (!g_mg.active) {
         fail(E_STATE, "ref_free_alignment_2D called before ref_free_alignment_2D_init");

@@ -94,6 +94,7 @@ normalize_mask_kernel(float* __restrict__ imgs, size_t pixels, const float* __re
 extern "C" int gpuisac_normalize_mask(float* imgs, unsigned int n_img, unsigned int img_dim, const float* mask,
                                       int no_sigma, void* stream)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:normalize_mask");
     if (n_img == 0)
         return 0;
     if (!imgs || !mask || img_dim == 0 || img_dim > 4096) {

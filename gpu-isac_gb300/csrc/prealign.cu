@@ -291,6 +291,7 @@ void pre_align_fetch(const float** img_data, unsigned int img_num, const char* b
 
 void pre_align_run(int start_idx, int stop_idx)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:pre_align_run");
     std::lock_guard<std::mutex> lk(g_pre.mu);
     PreState& s = g_pre;
     auto run = [&]() -> int {

@@ -281,6 +281,7 @@ extern "C" int gpuisac_learned_align_device(const AlignConfig* cfg, const float*
                                             float* best_peak, float* best_param, float* best_gap,
                                             unsigned int* fallback, unsigned long long* pairs, void* stream)
 {
+    const gpuisac::NvtxRange nvtx_range("gpuisac:learned_align");
     HostGeometry geo;
     int rc = host_geometry(cfg, geo);
     if (rc)

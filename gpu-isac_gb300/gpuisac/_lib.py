@@ -51,6 +51,7 @@ EXPORTS = (
     "gpuisac_ccf_tile_name", "gpuisac_nn_gemm_bf16", "gpuisac_assign_groups_device", "gpuisac_assign_groups",
     "gpuisac_ref_free_averages", "gpuisac_set_contraction", "gpuisac_get_contraction", "gpuisac_test_stall_ccf", "gpuisac_normalize_mask",
     "gpuisac_split_plan", "gpuisac_groups_stats", "gpuisac_checked_failures", "gpuisac_class_averages",
+    "gpuisac_test_fail_alloc",
 )
 
 
@@ -198,6 +199,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
     L.gpuisac_get_contraction.restype = ctypes.c_int
     L.gpuisac_test_stall_ccf.argtypes = [ctypes.c_uint]
     L.gpuisac_test_stall_ccf.restype = None
+    L.gpuisac_test_fail_alloc.argtypes = [ctypes.c_uint]
+    L.gpuisac_test_fail_alloc.restype = None
     L.gpuisac_normalize_mask.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p]
     L.gpuisac_normalize_mask.restype = ctypes.c_int

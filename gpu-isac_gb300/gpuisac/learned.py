@@ -30,6 +30,8 @@ from ._lib import GpuIsacError
 from .align import align_proposals_device, make_config
 
 NK = 16            # angular harmonics per ring fed to the network
+MODEL_FORMAT = "gpuisac-proposal-net"  # ProposalNet.save / load
+MODEL_VERSION = 1
 HIDDEN = 256
 EMB = 128
 SCALE = 16.0       # score = SCALE * cosine similarity of embeddings
@@ -135,6 +137,54 @@ class ProposalNet:
 
     def params(self) -> dict:
         return {k: self.view(self.flat, k).cpu().numpy().copy() for k in self.shapes}
+
+    # ---------------------------------------------------------------- files
+    def save(self, path: str, **meta) -> None:
+        """Weights and feature statistics to path + ".npz" (float32), the
+        architecture and any caller metadata (gap_margin, k, training notes:
+        JSON values) to path + ".json", with a format name and version."""
+        import hashlib
+        import json
+
+        arrays = dict(self.params(), mu=self.mu.cpu().numpy(), inv_sd=self.inv_sd.cpu().numpy())
+        np.savez(path + ".npz", **arrays)
+        with open(path + ".npz", "rb") as f:
+            digest = hashlib.sha256(f.read()).hexdigest()
+        doc = {"format": MODEL_FORMAT, "version": MODEL_VERSION, "ring_num": self.ring_num, "nk": self.nk,
+               "hidden": self.hidden, "emb": self.emb, "scale": self.scale, "n_params": self.n_params,
+               "weights_sha256": digest, "meta": meta}
+        with open(path + ".json", "w") as f:
+            json.dump(doc, f, indent=1, sort_keys=True)
+
+    @classmethod
+    def load(cls, path: str, device=None):
+        """The network save() wrote at path (".json" + ".npz"), on device.
+        Returns (net, meta).  Raises ValueError for another format or
+        version, weights that do not match their recorded digest, or arrays
+        of the wrong shapes."""
+        import hashlib
+        import json
+
+        with open(path + ".json") as f:
+            doc = json.load(f)
+        if doc.get("format") != MODEL_FORMAT or doc.get("version") != MODEL_VERSION:
+            raise ValueError(f"{path}.json: not a {MODEL_FORMAT} file of version {MODEL_VERSION}")
+        with open(path + ".npz", "rb") as f:
+            if hashlib.sha256(f.read()).hexdigest() != doc["weights_sha256"]:
+                raise ValueError(f"{path}.npz does not match the digest recorded in {path}.json")
+        net = cls(doc["ring_num"], nk=doc["nk"], hidden=doc["hidden"], emb=doc["emb"], scale=doc["scale"],
+                  device=device)
+        with np.load(path + ".npz") as z:
+            arrays = {k: z[k] for k in z.files}
+        want = dict(net.shapes, mu=(net.n_in,), inv_sd=(net.n_in,))
+        for k, shp in want.items():
+            if k not in arrays or tuple(arrays[k].shape) != tuple(shp):
+                raise ValueError(f"{path}.npz: {k} missing or not of shape {shp}")
+        net.load_params(arrays)
+        import torch
+        net.mu.copy_(torch.as_tensor(arrays["mu"].astype(np.float32)))
+        net.inv_sd.copy_(torch.as_tensor(arrays["inv_sd"].astype(np.float32)))
+        return net, doc["meta"]
 
     def grads(self) -> dict:
         return {k: self.view(self.grad, k).cpu().numpy().copy() for k in self.shapes}

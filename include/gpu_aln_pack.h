@@ -213,6 +213,12 @@ int gpuisac_multi_ref_align_device(const AlignConfig *cfg, const float *sbj, con
  * most 20 us, so that the call comes back with error code 1 ("timed out") and
  * the context stays usable; 0 restores normal operation. */
 void gpuisac_test_stall_ccf(unsigned int wait_iters);
+/* No counterpart in the reference (whose cudaMalloc failures exit the
+ * process): failure-path tests only -- the next n device allocations of the
+ * alignment's work space fail as if the device were out of memory, so that
+ * the call returns error code 5 (E_NOMEM, "injected") with nothing left
+ * allocated half-way; 0 cancels what is pending. */
+void gpuisac_test_fail_alloc(unsigned int n);
 
 #define GPUISAC_CONTRACTION_FP32 0
 #define GPUISAC_CONTRACTION_BF16X3 1

@@ -8,7 +8,8 @@ gpuisac_test_stall_ccf makes those kernels issue no copies -- a wait on a
 barrier that nothing completes -- with a short limit (64 tries of at most
 20 us), so the wait runs out with no copy outstanding.  The call must come
 back with the error, quickly, and the next normal call on the same context
-must give correct results.
+must give correct results.  Allocation failures are injected on the host
+(gpuisac_test_fail_alloc): the call reports them and the next call is right.
 """
 import os
 import time
@@ -72,3 +73,23 @@ def test_stalled_averaging_wait_returns_error_and_context_survives(gpulib, cuda,
     a_o, p_o, m_o, s_o = oracle_mod.class_averages(imgs, peaks, bel, 0.2, 0.2, True)
     assert np.abs(avg - a_o).max() < 2e-5 * np.abs(a_o).max()
     assert np.abs(prm - p_o).max() < 2e-6
+
+
+@pytest.mark.parametrize("n", [1, 4])
+def test_injected_allocation_failure_returns_error_and_next_call_works(gpulib, cuda, oracle_mod, stack, n):
+    """The alignment's work-space allocations fail as if the device were out
+    of memory (gpuisac_test_fail_alloc, on the host): the call reports it,
+    and the next call, with nothing injected, allocates and is right."""
+    from gpuisac import multi_ref_align
+    gpulib.gpu_clear()  # an empty work space: the next call allocates
+    gpulib.gpuisac_clear_error()
+    gpulib.gpuisac_test_fail_alloc(n)
+    try:
+        with pytest.raises(GpuIsacError, match="injected"):
+            multi_ref_align(stack.particles, stack.refs, 29, 2.0, 2.0)
+    finally:
+        gpulib.gpuisac_test_fail_alloc(0)
+        gpulib.gpuisac_clear_error()
+    pl, d = multi_ref_align(stack.particles, stack.refs, 29, 2.0, 2.0)
+    peak_o, d_o = oracle_run(oracle_mod, stack.particles, stack.refs, 29, 2.0, tex=gpulib.get_texture_limit(64))
+    compare(pl.reshape(6, 24, 4), d, peak_o, d_o)
