@@ -78,3 +78,39 @@ def test_config_parity_vs_fp64_oracle(gpulib, cuda, oracle_mod, name, mode):
     # the synthetic ground truth: the best reference is the particle's class
     # for nearly every particle at these SNRs
     assert (np.argmax(d, 0) == st.cls).mean() > 0.9
+
+
+def test_reference_test_main_configuration(gpulib, cuda, oracle_mod):
+    """The configuration of the reference library's own timing harness
+    (cuda/gpu_aln_noref.cu:2629-2637: 76^2 images, 110 references, 29 rings,
+    shifts +-1, images of rand() % 255), on 1,000 of its 11,003 particles:
+    un-normalised integer images in 0..254 with no structure, both
+    contractions against the FP64 oracle, with the bars of the structured
+    workloads (measured on GB300: 7.2e-7 / 5.7e-6 max relative peak error,
+    every best pair and every tuple the same)."""
+    import oracle
+
+    from gpuisac import multi_ref_align
+    rng = np.random.default_rng(2637)
+    P, R, D, NR = 1000, 110, 76, 29
+    parts = rng.integers(0, 255, (P, D, D)).astype(np.float32)
+    refs = rng.integers(0, 255, (R, D, D)).astype(np.float32)
+    cfg = oracle.make_cfg(P, R, D, NR, 256, 1.0, 1.0, 1.0)
+    lay = oracle.reference_layout(cfg)
+    lay = oracle.OrcLayout(lay.sbj_batch, gpulib.get_texture_limit(D), lay.ref_batch)
+    peak_o, d_o = oracle_mod.multi_ref_align(cfg, lay, parts, refs, precision="f64")
+    peak_o, d_o = np.asarray(peak_o), np.asarray(d_o, np.float64).reshape(R, P)
+    from test_gpu_align import ANGLE_TOL, PEAK_RTOL, SAME_BEST, SAME_PAIR, circ_diff
+    for mode in ("fp32", "bf16x3"):
+        pl, d = multi_ref_align(parts, refs, NR, 1.0, 1.0, contraction_mode=mode)
+        pg = pl.reshape(R, P, 4)
+        floor = NEAR_ZERO * cs_bound(NR, 256)
+        rel = np.abs(d.astype(np.float64) - d_o) / np.maximum(np.abs(d_o), floor)
+        same = (pg[..., 1:] == peak_o[..., 1:]).all(-1) & (circ_diff(pg[..., 0], peak_o[..., 0]) < ANGLE_TOL)
+        qg, qo = np.argmax(d, 0), np.argmax(d_o, 0)
+        best = ((qg == qo) & same[qo, np.arange(P)]).mean()
+        print(f"reference harness configuration, {mode}: max rel peak err {rel.max():.2e}, same best {best:.4f}, "
+              f"same tuples {same.mean():.4f}")
+        assert rel.max() <= PEAK_RTOL
+        assert best >= SAME_BEST
+        assert same.mean() >= SAME_PAIR
