@@ -940,6 +940,8 @@ void gpu_clear(void)
     }
     gpuisac::prealign_clear();
     gpuisac::multigroup_clear();
+    gpuisac::assign_clear();
+    gpuisac::averages_clear();
     gpuisac::release_upload_staging();
 }
 

@@ -594,6 +594,25 @@ int assign_locked(const float* d, size_t pitch, unsigned nref, unsigned nima, in
 }
 
 } // namespace
+
+void assign_clear()
+{
+    std::lock_guard<std::mutex> lk(g_asg.mu);
+    AssignState& w = g_asg;
+    auto drop = [](auto& b) {
+        if (b.p)
+            cudaFree(b.p);
+        b.p = nullptr;
+        b.n = 0;
+    };
+    drop(w.theta), drop(w.pkey), drop(w.bk), drop(w.cnt), drop(w.touched), drop(w.off), drop(w.fill);
+    drop(w.bp), drop(w.list), drop(w.sc), drop(w.redo), drop(w.assign), drop(w.d_host_copy);
+    drop(w.ids_host_copy);
+    if (w.h_sc)
+        cudaFreeHost(w.h_sc);
+    w.h_sc = nullptr;
+}
+
 } // namespace gpuisac
 
 using namespace gpuisac;

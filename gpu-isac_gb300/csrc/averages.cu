@@ -706,6 +706,16 @@ void release(AvgState& w)
 
 GPUISAC_CHECKED_READER(checked_read_averages)
 
+void averages_clear()
+{
+    std::lock_guard<std::mutex> lk(g_avg.mu);
+    release(g_avg);
+    g_avg.dev = -1;
+    if (g_avg.h_err)
+        cudaFreeHost(g_avg.h_err);
+    g_avg.h_err = nullptr;
+}
+
 } // namespace gpuisac
 
 using namespace gpuisac;

@@ -69,4 +69,9 @@ void release_upload_staging();
 int multigroup_reset_shifts(float shift_range, float shift_step);
 void multigroup_clear();
 
+// The work spaces of the group assignment (assign.cu) and of the averaging
+// step (averages.cu), released by gpu_clear.
+void assign_clear();
+void averages_clear();
+
 } // namespace gpuisac

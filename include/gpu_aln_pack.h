@@ -63,7 +63,10 @@ AlignParam *multi_ref_align_init(const AlignConfig *aln_cfg, unsigned int cuda_d
 void multi_ref_align(const float **sbj_data, const float **ref_data, float *isac_peak_list, float *isac_d,
                      unsigned int isac_d_pitch, float cuda_mem_request);
 
-/* Replaces gpu_clear, cuda/gpu_aln_noref.h:57 / cuda/gpu_aln_noref.cu:139-180. */
+/* Replaces gpu_clear, cuda/gpu_aln_noref.h:57 / cuda/gpu_aln_noref.cu:139-180:
+ * ends the open sessions and frees the library's device and pinned memory,
+ * including the work spaces of this library's additions (group assignment,
+ * averaging step, host staging). */
 void gpu_clear(void);
 
 /* Replaces reset_shifts, cuda/gpu_aln_noref.cu:117-137: rebuilds the shift

@@ -104,12 +104,20 @@ def test_more_groups_than_shared_memory_counts(gpulib, cuda, oracle_mod):
 
 
 def test_repeat_calls_identical(gpulib, cuda):
+    """Repeat calls give the same bits, also after gpu_clear released the
+    step's work space (and the group assignment's)."""
+    from gpuisac.assign import assign_groups
     from gpuisac.averages import class_averages
     imgs, peaks, bel = _case(500, 7, 76, 4)
     a = class_averages(imgs, peaks, bel, 0.2, 0.2, True)
     b = class_averages(imgs, peaks, bel, 0.2, 0.2, True)
-    for x, y in zip(a, b):
-        assert np.array_equal(x, y)
+    d = np.random.default_rng(4).uniform(0.0, 1.0, (7, 500)).astype(np.float32)
+    ids = assign_groups(d, 7, 500)
+    gpulib.gpu_clear()
+    c = class_averages(imgs, peaks, bel, 0.2, 0.2, True)
+    for x, y, z in zip(a, b, c):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
+    assert assign_groups(d, 7, 500) == ids
 
 
 def test_errors(gpulib, cuda, oracle_mod):
