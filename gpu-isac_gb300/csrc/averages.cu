@@ -351,6 +351,7 @@ avg_sum_kernel(AvgSumArgs a)
 {
     extern __shared__ __align__(16) float sbuf[];
     __shared__ uint64_t bars[2];
+    __shared__ AvgMember mrec[2]; // the member whose image a buffer holds (written with the copy's issue)
     const unsigned t = blockIdx.x, R = a.R, D = a.D, G = a.G;
     const unsigned n_pieces = a.pstart[R];
     if (t >= n_pieces)
@@ -375,6 +376,7 @@ avg_sum_kernel(AvgSumArgs a)
         if (a.test_stall)
             return; // failure-path test: no copy, a wait that runs out
         const AvgMember b = a.rec[a.order[k]];
+        mrec[buf] = b; // published to the other threads by the arrive below (release) and their wait (acquire)
         if (GPUISAC_IN_BOUNDS(kChkAvgImg, b.img, a.P)) {
             mbar_expect_tx(&bars[buf], bytes);
             bulk_g2s(sbuf + buf * npix, a.imgs + (size_t)b.img * npix, bytes, &bars[buf]);
@@ -407,7 +409,7 @@ avg_sum_kernel(AvgSumArgs a)
                 const unsigned buf = u & 1u;
                 const bool ok = mbar_wait(&bars[buf], (u >> 1) & 1u, wlim);
                 if (ok)
-                    accumulate(acc, sbuf + buf * npix, a.rec[a.order[k]], ix, row0 + g, G, D);
+                    accumulate(acc, sbuf + buf * npix, mrec[buf], ix, row0 + g, G, D);
                 if (__syncthreads_or(!ok)) {
                     if (tid == 0) {
                         atomicAdd(a.err + kErrWait, 1u);
