@@ -163,3 +163,24 @@ def test_assign_groups_rejects_bad_arguments_on_the_host(lib):
     code, msg = _lib.last_error(lib)
     assert code == 2 and "assign_groups" in msg
     lib.gpuisac_clear_error()
+
+
+def test_class_averages_rejects_bad_arguments_on_the_host(lib):
+    """gpuisac_class_averages checks its arguments before any device call:
+    each refusal is error 2 with a message (the pointers are never read)."""
+    from gpuisac import _lib
+    p = 1 << 20  # a 16-byte aligned address the refusals never dereference
+    f = lib.gpuisac_class_averages
+    lib.gpuisac_clear_error()
+    assert f(None, 10, 8, p, 0, p, 3, 0.2, 0.2, 1, p, p, None, None, None) == 2   # no images
+    assert f(p, 0, 8, p, 0, p, 3, 0.2, 0.2, 1, p, p, None, None, None) == 2      # no particles
+    assert f(p, 10, 8, p, 0, p, 0, 0.2, 0.2, 1, p, p, None, None, None) == 2     # no groups
+    assert f(p, 10, 300, p, 0, p, 3, 0.2, 0.2, 1, p, p, None, None, None) == 2   # side above 256
+    assert f(p, 10, 8, p, 5, p, 3, 0.2, 0.2, 1, p, p, None, None, None) == 2     # pitch below n_img
+    assert f(p, 10, 8, p + 4, 0, p, 3, 0.2, 0.2, 1, p, p, None, None, None) == 2  # peaks misaligned
+    assert f(p, 10, 8, p, 0, p, 3, 0.7, 0.2, 1, p, p, None, None, None) == 2     # cut-off above Nyquist
+    assert f(p, 10, 8, p, 0, p, 3, 0.2, -0.1, 1, p, p, None, None, None) == 2    # negative fall-off
+    assert f(p, 10, 8, p, 0, p, 3, 0.2, 0.2, 1, p, p + 8, None, None, None) == 2  # params misaligned
+    code, msg = _lib.last_error(lib)
+    assert code == 2 and "class_averages" in msg
+    lib.gpuisac_clear_error()
