@@ -20,7 +20,8 @@
 //  6. avg_shift_kernel       one warp per group: mean shifts, parameters
 //  7. avg_sum_kernel         one CTA per piece (a run of one group's members):
 //                            each member image staged in shared memory by a
-//                            bulk copy (two buffers), every thread one column
+//                            bulk copy (two buffers, the member's record
+//                            written beside it), every thread one column
 //                            and every G-th row of the output, the quadratic
 //                            interpolation from shared memory, FP32 sums in
 //                            registers, one partial image per piece
